@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Benchmark: site updates/s of the batched parallel-tempering sweep.
+
+Workload (the single-GPU headline configuration): simple-cubic Heisenberg
+model, L=24 (13824 sites), J=+I on the 6 nearest neighbours, onsite D*Sz^2
+with D=0.2, S=1; 64 replicas on a geometric temperature ladder 0.1..2.0;
+overrelaxation_rate=5 (1 Metropolis + 5 overrelaxation sweeps), exchanges
+every 10 sweeps, probes every 10 sweeps.  Spins, fields and dE in FP32;
+energies, the exchange exponent and observables in FP64.  Synthetic: random
+initial spins from the Philox INIT stream.
+
+One step = one exchange window of the reference's loop (monte_carlo.jl:295-388):
+10 iterations = 10 overrelaxation + 2 Metropolis sweeps of all 64 replicas,
+the energies, one replica exchange and one probe (E, |M|).
+Site updates per step = 64 * 13824 * 12.
+
+`value` is device throughput (CUDA events on the library's stream) with the
+replicas resident in HBM; L2 is flushed (256 MB write) between steps.
+`e2e` goes through the public C ABI with host buffers every step:
+csmc_set_spins_all (FP64 reference layout, all replicas) -> csmc_run ->
+csmc_get_spins_all + probe records.
+
+--impl reference times the CPU restatement of the reference's algorithm
+(the oracle: random-site Metropolis, sequential overrelaxation, total energy
+after every Metropolis sweep, in-process replica exchange) on all host cores,
+one replica per thread, on a bounded sample of the same workload.
+Multi-GPU (torchrun): independent replica sets per GPU, no collective on the
+data path ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+import __graft_entry__ as G  # noqa: E402
+
+L_SIDE, R_REPL, OR_RATE, SWAP_RATE, PROBE_RATE = 24, 64, 5, 10, 10
+ITER_PER_STEP = 10
+SEED = 20261203
+BYTES_PER_UPDATE_FP32 = 12 * (2 + 6)  # s_b * (2 + z): own spin read+write, 6 neighbours read
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "sc_heisenberg_onsite_pt", "lattice": "simple cubic L=24 (13824 sites)", "replicas": R_REPL,
+           "T_ladder": "geometric 0.1..2.0", "overrelaxation_rate": OR_RATE, "swap_rate": SWAP_RATE,
+           "probe_rate": PROBE_RATE, "iterations_per_step": ITER_PER_STEP,
+           "site_updates_per_step": R_REPL * L_SIDE ** 3 * (ITER_PER_STEP + ITER_PER_STEP // OR_RATE),
+           "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def temperatures():
+    return np.exp(np.linspace(math.log(0.1), math.log(2.0), R_REPL))
+
+
+def make_lattice(m):
+    return m.Lattice((L_SIDE,) * 3, m.examples.sc_heisenberg(J=1.0, D=0.2), 1.0, initialCondition="none")
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.rows, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 3 + k and r[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def run_params(L, start, n, rec_E=None, rec_M=None, cap=0, path=0):
+    rp = L.RunParams()
+    rp.sweep_start = start
+    rp.n_sweeps = n
+    rp.t_thermalization = 0
+    rp.overrelaxation_rate = OR_RATE
+    rp.swap_rate = SWAP_RATE
+    rp.probe_rate = PROBE_RATE
+    rp.kind = L.METROPOLIS
+    rp.path = path
+    if rec_E is not None:
+        rp.probe_energy = rec_E.ctypes.data_as(C.POINTER(C.c_double))
+        rp.probe_magnetization = rec_M.ctypes.data_as(C.POINTER(C.c_double))
+        rp.probe_capacity = cap
+    return rp
+
+
+def stats(ctx):
+    ms, n, kms, kn = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
+    ctx.call("csmc_last_run_stats", C.byref(ms), C.byref(n), C.byref(kms), C.byref(kn))
+    return ms.value, n.value, kms.value, kn.value
+
+
+def bench_ours(args, rank, world, dist):
+    import torch
+    m = G.load()
+    from importlib import import_module
+    L = import_module(m.__name__ + "._lib")
+    dev = rank % max(torch.cuda.device_count(), 1)
+    torch.cuda.set_device(dev)
+    lat = make_lattice(m)
+    ctx = m.monte_carlo.Context([lat], [R_REPL], precision="fp32", seed=SEED + rank)
+    ctx.set_temperatures(temperatures())
+    ctx.call("csmc_random_spins", C.c_uint64(SEED + 1000 * rank))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    upd = R_REPL * lat.size * (ITER_PER_STEP + ITER_PER_STEP // OR_RATE)
+    it = 1  # steps cover iterations [10k+1, 10k+10]: one exchange window each
+    for _ in range(args.warmup):
+        ctx.call("csmc_run", C.byref(run_params(L, it, ITER_PER_STEP)))
+        it += ITER_PER_STEP
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    dev_ms = kern_ms = 0.0
+    launches = kern_launches = 0
+    barrier()
+    with Clocks(dev) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ctx.call("csmc_run", C.byref(run_params(L, it, ITER_PER_STEP)))
+            it += ITER_PER_STEP
+            a, b, c, d = stats(ctx)
+            dev_ms += a
+            launches += b
+            kern_ms += c
+            kern_launches += d
+        barrier()
+        wall = time.perf_counter() - t0
+    t_dev = dev_ms / 1e3
+    if dist:
+        tt = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = world * upd * args.steps / t_dev
+    out = {"value": value, "ms_per_step": 1e3 * t_dev / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
+           "gpu_launches": launches, "clocks": clk.summary()}
+    # roofline of the dominant kernel (the resident sweep kernel, one launch per step)
+    per_launch_s = kern_ms / 1e3 / max(kern_launches, 1)
+    bytes_per_launch = upd * BYTES_PER_UPDATE_FP32 * args.steps / max(kern_launches, 1)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = bytes_per_launch / per_launch_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("k_resident_fp32_sc_L24_R64")
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "traffic": traffic, "kernel": "k_resident<float>",
+                       "kernel_ms_per_launch": per_launch_s * 1e3, "algorithmic_bytes_per_launch": bytes_per_launch,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"}
+
+    # end to end through the C ABI with host buffers
+    nh = R_REPL * lat.size * 3
+    h_in = torch.empty(nh, dtype=torch.float64).pin_memory().numpy()
+    h_out = torch.empty(nh, dtype=torch.float64).pin_memory().numpy()
+    ctx.call("csmc_get_spins_all", h_in.ctypes.data_as(C.POINTER(C.c_double)))
+    cap = ITER_PER_STEP // PROBE_RATE + 2
+    rec_E = np.zeros((cap, R_REPL))
+    rec_M = np.zeros((cap, R_REPL))
+    e2e_steps = max(3, min(args.steps, args.e2e_steps))
+    for k in range(e2e_steps + 2):
+        if k == 2:
+            barrier()
+            t0 = time.perf_counter()
+        ctx.call("csmc_set_spins_all", h_in.ctypes.data_as(C.POINTER(C.c_double)))
+        ctx.call("csmc_run", C.byref(run_params(L, it, ITER_PER_STEP, rec_E, rec_M, cap)))
+        it += ITER_PER_STEP
+        ctx.call("csmc_get_spins_all", h_out.ctypes.data_as(C.POINTER(C.c_double)))
+        h_in, h_out = h_out, h_in
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    out["e2e"] = {"value": world * upd * e2e_steps / t_e2e, "unit": "site updates/s",
+                  "h2d_bytes_per_step": nh * 8, "d2h_bytes_per_step": nh * 8 + 2 * cap * R_REPL * 8,
+                  "ms_per_step": 1e3 * t_e2e / e2e_steps,
+                  "api": "csmc_set_spins_all + csmc_run + csmc_get_spins_all"}
+
+    # the plain FP64 one-replica-per-launch path on the same workload (spec comparison)
+    if rank == 0 and args.plain_steps > 0:
+        ctx64 = m.monte_carlo.Context([lat], [R_REPL], precision="fp64", seed=SEED)
+        ctx64.set_temperatures(temperatures())
+        ctx64.call("csmc_random_spins", C.c_uint64(SEED))
+        ctx64.call("csmc_run", C.byref(run_params(L, 1, ITER_PER_STEP, path=L.PATH_PER_REPLICA)))
+        t = 0.0
+        for k in range(args.plain_steps):
+            ctx64.call("csmc_run", C.byref(run_params(L, 11 + 10 * k, ITER_PER_STEP, path=L.PATH_PER_REPLICA)))
+            t += stats(ctx64)[0] / 1e3
+        out["plain_fp64_per_replica"] = {"value": upd * args.plain_steps / t, "unit": "site updates/s",
+                                         "ms_per_step": 1e3 * t / args.plain_steps,
+                                         "batched_fp32_speedup": value / world / (upd * args.plain_steps / t)}
+    return out
+
+
+def oracle_sample(target_s: float, threads: int):
+    """The oracle's parallel tempering on the same workload; returns updates/s and the sample."""
+    m = G.load()
+    orc = G.load_oracle()
+    uc = m.examples.sc_heisenberg(J=1.0, D=0.2)
+    ol = orc.OracleLattice(uc, (L_SIDE,) * 3, 1.0)
+    spins = [ol.random_spins(SEED, r) for r in range(R_REPL)]
+    T = temperatures()
+
+    def run(n_iter):
+        t0 = time.perf_counter()
+        ol.parallel_tempering(spins, T, 0, n_iter, PROBE_RATE, SWAP_RATE, OR_RATE, n_threads=threads, seed=SEED)
+        return time.perf_counter() - t0
+
+    t1 = run(ITER_PER_STEP)
+    n = max(ITER_PER_STEP, int(round(target_s / max(t1, 1e-6) * ITER_PER_STEP / 10.0)) * 10)
+    t = run(n)
+    upd = R_REPL * ol.N * (n + n // OR_RATE)
+    return upd / t, {"iterations": n, "seconds": t,
+                     "sample": f"{n} iterations (= {n // ITER_PER_STEP} steps) of the 64-replica L=24 workload"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    threads = os.cpu_count() or 1
+    metric = "site updates/s (Metropolis+OR), batched FP32 vs plain FP64 GPU, |dE/N|<=1e-4"
+    unit = "site updates/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        v, sample = oracle_sample(args.cpu_seconds, threads)
+        line = {"metric": metric, "value": v, "unit": unit, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config({"parallelism": "threads (one replica per thread)"}),
+                "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
+                                 "sample": sample["sample"]},
+                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    dist = world > 1
+    if dist:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res = bench_ours(args, rank, world, dist)
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1:
+        v, sample = oracle_sample(args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": unit, "cores": threads, "kind": "port", "sample": sample["sample"]}
+    line = {"metric": metric, "value": res["value"], "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config({"precision": "FP32 spins/fields/dE, FP64 energies+exchange+observables",
+                                       "wall_ms_per_step": res["wall_ms_per_step"]}),
+            "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "clocks": res["clocks"],
+            "gpu_launches": res["gpu_launches"]}
+    if "plain_fp64_per_replica" in res:
+        line["plain_fp64_per_replica"] = res["plain_fp64_per_replica"]
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

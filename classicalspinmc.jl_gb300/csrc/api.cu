@@ -1,0 +1,1201 @@
+// api.cu -- the C ABI of libcsmc.so (include/csmc.h): contexts, host<->device
+// layout conversion, and the multi-sweep drivers that schedule the kernels of
+// kernels.cu in the cadence of simulated_annealing! / parallel_tempering!
+// (monte_carlo.jl:157-190, :288-388).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "launch.hpp"
+#include "plan.hpp"
+
+namespace csmc {
+
+static thread_local std::string g_err;
+
+#define CK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess)                                                                                         \
+            throw Error(e_ == cudaErrorMemoryAllocation ? CSMC_ERR_OOM : CSMC_ERR_CUDA,                                \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                           \
+    } while (0)
+
+static void require(bool ok, int code, const std::string &msg) {
+    if (!ok) throw Error(code, msg);
+}
+
+template <typename T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t count) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = count;
+        if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+    }
+    void upload(const T *src, size_t count) {
+        alloc(count);
+        if (count) CK(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    template <class V> void upload(const V &v) { upload(v.data(), v.size()); }
+    void zero(cudaStream_t st) {
+        if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+    }
+};
+
+struct System {
+    Plan plan;
+    int R = 0, base = 0; // replicas, first chain/slot
+    bool cub = false, qua = false;
+    DevBuf<uint32_t> p2, p3, p4;
+    DevBuf<uint16_t> q2, q3, q4;
+    DevBuf<uint8_t> pat;
+    DevBuf<int32_t> dev2ref, c2, c3, c4;
+    DevBuf<int64_t> ref2dev;
+    DevBuf<float> fmats, fcubs, fquas, fO, fP, fh, fspins;
+    DevBuf<double> dmats, dcubs, dquas, dO, dP, dh, dspins;
+    SysArgs<float> fa{};
+    SysArgs<double> da{};
+    bool resident_ok = false;
+    size_t resident_smem = 0;
+    // reference-layout tables for the replay kernel (built on first use)
+    DevBuf<int64_t> xbs, xcs, xqs;
+    DevBuf<double> xbm, xct, xqt, xfield, xonsite;
+    bool exact_ready = false;
+};
+
+struct Ctx {
+    int precision = CSMC_FP64;
+    uint64_t seed = 0;
+    uint32_t k0 = 0, k1 = 0;
+    int device = 0, n_sms = 0, max_smem = 0;
+    std::vector<std::unique_ptr<System>> sys;
+    int n_chains = 0;
+    cudaStream_t st = nullptr;
+    DevBuf<int32_t> slot_of, chain_of;
+    DevBuf<double> T_slot, sigma_slot, acc_slot, exch_slot, E_chain, M_chain, last_acc;
+    DevBuf<unsigned long long> sweep_acc;
+    DevBuf<unsigned int> drift_bits;
+    DevBuf<int> error_flag, work_ctr;
+    DevBuf<double> part, stage, rec_E, rec_M;
+    DevBuf<ResSys<float>> fres;
+    DevBuf<ResSys<double>> dres;
+    DevBuf<int2> items;
+    int n_items = 0;
+    uint32_t msweep = 0;
+    int renorm_every = 64;
+    double last_ms = 0.0;
+    int64_t last_launches = 0;
+    // CUDA events bracketing each resident-kernel launch of the current run
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kev;
+    size_t kev_used = 0;
+    double last_kernel_ms = 0.0;
+    int64_t last_kernel_launches = 0;
+    ChainState cs{};
+
+    ~Ctx() {
+        for (auto &e : kev) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+        if (st) cudaStreamDestroy(st);
+    }
+    std::pair<cudaEvent_t, cudaEvent_t> next_kernel_events() {
+        if (kev_used == kev.size()) {
+            std::pair<cudaEvent_t, cudaEvent_t> e;
+            CK(cudaEventCreate(&e.first));
+            CK(cudaEventCreate(&e.second));
+            kev.push_back(e);
+        }
+        return kev[kev_used++];
+    }
+    void reset_kernel_time() {
+        kev_used = 0;
+        last_kernel_ms = 0.0;
+        last_kernel_launches = 0;
+    }
+    // after the stream has been synchronised: add the time of the bracketed launches
+    void collect_kernel_time() {
+        for (size_t k = 0; k < kev_used; k++) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, kev[k].first, kev[k].second));
+            last_kernel_ms += ms;
+        }
+        last_kernel_launches += (int64_t)kev_used;
+        kev_used = 0;
+    }
+    int sys_of_slot(int slot) const {
+        for (size_t k = 0; k < sys.size(); k++)
+            if (slot >= sys[k]->base && slot < sys[k]->base + sys[k]->R) return (int)k;
+        throw Error(CSMC_ERR_INVALID, "slot " + std::to_string(slot) + " out of range");
+    }
+};
+
+template <typename V> static std::vector<float> to_f(const V &v) { return std::vector<float>(v.begin(), v.end()); }
+
+static void upload_system(Ctx &C, System &S) {
+    const Plan &P = S.plan;
+    const int nb = P.desc.nb;
+    S.p2.upload(P.p2);
+    S.p3.upload(P.p3);
+    S.p4.upload(P.p4);
+    S.pat.upload(P.pat);
+    std::vector<int32_t> d2r(P.dev2ref.begin(), P.dev2ref.end());
+    S.dev2ref.upload(d2r);
+    S.ref2dev.upload(P.ref2dev);
+    S.c2.upload(P.c2);
+    S.c3.upload(P.c3);
+    S.c4.upload(P.c4);
+    // per-pattern onsite, folded self loops and field; pattern nb is padding
+    std::vector<double> O((nb + 1) * 9, 0.0), Pm((nb + 1) * 9, 0.0), h((nb + 1) * 3, 0.0);
+    for (int b = 0; b < nb; b++) {
+        for (int k = 0; k < 9; k++) {
+            O[b * 9 + k] = P.onsite_b[b][k];
+            Pm[b * 9 + k] = P.self_b[b][k];
+        }
+        for (int k = 0; k < 3; k++) h[b * 3 + k] = P.field_b[b][k];
+    }
+    S.cub = P.W3 > 0;
+    S.qua = P.W4 > 0;
+    const int64_t Np = P.Np;
+    if (P.Np <= 65536) {
+        std::vector<uint16_t> a(P.p2.begin(), P.p2.end()), b(P.p3.begin(), P.p3.end()), c(P.p4.begin(), P.p4.end());
+        S.q2.upload(a);
+        S.q3.upload(b);
+        S.q4.upload(c);
+    }
+    auto fill_args = [&](auto &a, auto *spins, auto *mats, auto *cubs, auto *quas, auto *Oo, auto *Pp, auto *hh) {
+        a.tb.p2 = S.p2.p;
+        a.tb.p3 = S.p3.p;
+        a.tb.p4 = S.p4.p;
+        a.tb.pat = S.pat.p;
+        a.tb.Np = Np;
+        a.tb.W2 = P.W2;
+        a.tb.W3 = P.W3;
+        a.tb.W4 = P.W4;
+        a.cf.mats = mats;
+        a.cf.cubs = cubs;
+        a.cf.quas = quas;
+        a.cf.O = Oo;
+        a.cf.P = Pp;
+        a.cf.h = hh;
+        a.cf.c2 = S.c2.p;
+        a.cf.c3 = S.c3.p;
+        a.cf.c4 = S.c4.p;
+        a.spins = spins;
+        a.dev2ref = S.dev2ref.p;
+        a.ref2dev = S.ref2dev.p;
+        a.chain_base = S.base;
+        a.n_rep = S.R;
+        a.n_real = P.N;
+        a.k0 = C.k0;
+        a.k1 = C.k1;
+        a.cub = S.cub;
+        a.qua = S.qua;
+    };
+    const size_t nsp = (size_t)S.R * 3 * Np;
+    if (C.precision == CSMC_FP32) {
+        S.fmats.upload(to_f(P.mats));
+        S.fcubs.upload(to_f(P.cubs));
+        S.fquas.upload(to_f(P.quas));
+        S.fO.upload(to_f(O));
+        S.fP.upload(to_f(Pm));
+        S.fh.upload(to_f(h));
+        S.fspins.alloc(nsp);
+        CK(cudaMemset(S.fspins.p, 0, nsp * sizeof(float)));
+        fill_args(S.fa, S.fspins.p, S.fmats.p, S.fcubs.p, S.fquas.p, S.fO.p, S.fP.p, S.fh.p);
+        S.fa.S = (float)P.desc.S;
+        S.resident_smem = 3 * Np * sizeof(float);
+    } else {
+        S.dmats.upload(P.mats);
+        S.dcubs.upload(P.cubs);
+        S.dquas.upload(P.quas);
+        S.dO.upload(O);
+        S.dP.upload(Pm);
+        S.dh.upload(h);
+        S.dspins.alloc(nsp);
+        CK(cudaMemset(S.dspins.p, 0, nsp * sizeof(double)));
+        fill_args(S.da, S.dspins.p, S.dmats.p, S.dcubs.p, S.dquas.p, S.dO.p, S.dP.p, S.dh.p);
+        S.da.S = P.desc.S;
+        S.resident_smem = 3 * Np * sizeof(double);
+    }
+    S.resident_ok = P.Np <= 65536 && (int64_t)S.resident_smem <= (int64_t)C.max_smem - 1024 &&
+                    P.n_colours <= CSMC_MAX_COLOURS;
+}
+
+template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R> &a) {
+    ResSys<R> r{};
+    r.tb.p2 = S.q2.p;
+    r.tb.p3 = S.q3.p;
+    r.tb.p4 = S.q4.p;
+    r.tb.pat = S.pat.p;
+    r.tb.Np = a.tb.Np;
+    r.tb.W2 = a.tb.W2;
+    r.tb.W3 = a.tb.W3;
+    r.tb.W4 = a.tb.W4;
+    r.cf = a.cf;
+    r.spins = a.spins;
+    r.chain_base = a.chain_base;
+    r.n_rep = a.n_rep;
+    r.n_colours = S.plan.n_colours;
+    r.nb = S.plan.desc.nb;
+    for (int c = 0; c <= S.plan.n_colours; c++) r.col_start[c] = S.plan.col_start[c];
+    for (int c = 0; c < S.plan.n_colours; c++) r.col_count[c] = S.plan.col_count[c];
+    r.n_real = S.plan.N;
+    r.S = a.S;
+    r.k0 = a.k0;
+    r.k1 = a.k1;
+    return r;
+}
+
+static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, int precision, uint64_t seed) {
+    require(n >= 1, CSMC_ERR_INVALID, "need at least one lattice");
+    require(precision == CSMC_FP32 || precision == CSMC_FP64, CSMC_ERR_INVALID, "precision must be CSMC_FP32 or CSMC_FP64");
+    std::unique_ptr<Ctx> C(new Ctx());
+    C->precision = precision;
+    C->seed = seed;
+    C->k0 = (uint32_t)seed;
+    C->k1 = (uint32_t)(seed >> 32);
+    int chains = 0;
+    for (int k = 0; k < n; k++) { // host-side validation and flattening first
+        require(reps[k] >= 1, CSMC_ERR_INVALID, "replica count must be >= 1");
+        auto S = std::make_unique<System>();
+        S->plan = make_plan(&descs[k]);
+        S->R = reps[k];
+        S->base = chains;
+        chains += reps[k];
+        C->sys.push_back(std::move(S));
+    }
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    require(ndev > 0, CSMC_ERR_CUDA, "no CUDA device");
+    CK(cudaGetDevice(&C->device));
+    CK(cudaDeviceGetAttribute(&C->n_sms, cudaDevAttrMultiProcessorCount, C->device));
+    CK(cudaDeviceGetAttribute(&C->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, C->device));
+    CK(cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking));
+    C->n_chains = chains;
+    for (auto &S : C->sys) upload_system(*C, *S);
+
+    const int nc = chains;
+    std::vector<int32_t> ident(nc);
+    std::iota(ident.begin(), ident.end(), 0);
+    C->slot_of.upload(ident);
+    C->chain_of.upload(ident);
+    std::vector<double> ones(nc, 1.0), sig(nc, 60.0), zeros(nc, 0.0);
+    C->T_slot.upload(ones);
+    C->sigma_slot.upload(sig);
+    C->acc_slot.upload(zeros);
+    C->exch_slot.upload(zeros);
+    C->E_chain.upload(zeros);
+    C->M_chain.upload(zeros);
+    C->last_acc.upload(zeros);
+    std::vector<unsigned long long> z64(nc, 0ull);
+    C->sweep_acc.upload(z64);
+    unsigned int zb = 0;
+    C->drift_bits.upload(&zb, 1);
+    int zi = 0;
+    C->error_flag.upload(&zi, 1);
+    C->work_ctr.upload(&zi, 1);
+    size_t part = 0, stage = 0;
+    for (auto &S : C->sys) {
+        part = std::max(part, (size_t)(3 * S->R * partial_blocks(S->plan.Np)));
+        stage = std::max(stage, (size_t)(3 * S->R * S->plan.N));
+    }
+    C->part.alloc(part);
+    C->stage.alloc(stage);
+    ChainState &cs = C->cs;
+    cs.slot_of = C->slot_of.p;
+    cs.chain_of = C->chain_of.p;
+    cs.T_slot = C->T_slot.p;
+    cs.sigma_slot = C->sigma_slot.p;
+    cs.acc_slot = C->acc_slot.p;
+    cs.exch_slot = C->exch_slot.p;
+    cs.E_chain = C->E_chain.p;
+    cs.M_chain = C->M_chain.p;
+    cs.sweep_acc = C->sweep_acc.p;
+    cs.drift_bits = C->drift_bits.p;
+    cs.error_flag = C->error_flag.p;
+
+    // resident descriptors and the work list (largest replicas first)
+    std::vector<ResSys<float>> fr;
+    std::vector<ResSys<double>> dr;
+    std::vector<int2> items;
+    for (size_t k = 0; k < C->sys.size(); k++) {
+        System &S = *C->sys[k];
+        if (precision == CSMC_FP32) fr.push_back(make_res(S, S.fa));
+        else dr.push_back(make_res(S, S.da));
+        for (int r = 0; r < S.R; r++) items.push_back(make_int2((int)k, r));
+    }
+    std::stable_sort(items.begin(), items.end(), [&](int2 a, int2 b) {
+        return C->sys[a.x]->plan.Np > C->sys[b.x]->plan.Np;
+    });
+    if (precision == CSMC_FP32) C->fres.upload(fr);
+    else C->dres.upload(dr);
+    C->items.upload(items);
+    C->n_items = (int)items.size();
+    CK(cudaDeviceSynchronize());
+    return C.release();
+}
+
+// ------------------------------------------------------------ helpers
+
+static void sync_check(Ctx &C) {
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaGetLastError());
+    int flag = 0;
+    CK(cudaMemcpy(&flag, C.error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        int z = 0;
+        CK(cudaMemcpy(C.error_flag.p, &z, sizeof(int), cudaMemcpyHostToDevice));
+        throw Error(CSMC_ERR_TIMEOUT, "a bounded device wait gave up (TMA staging did not complete)");
+    }
+}
+
+static std::vector<int32_t> download_i32(const DevBuf<int32_t> &b) {
+    std::vector<int32_t> v(b.n);
+    if (b.n) CK(cudaMemcpy(v.data(), b.p, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return v;
+}
+static std::vector<double> download_f64(const DevBuf<double> &b, size_t n) {
+    std::vector<double> v(n);
+    if (n) CK(cudaMemcpy(v.data(), b.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return v;
+}
+
+// Apply f(System&, args) with the context's arithmetic type.
+template <class F> static void with_args(Ctx &C, System &S, F &&f) {
+    if (C.precision == CSMC_FP32) f(S.fa);
+    else f(S.da);
+}
+
+static void set_spins_slot(Ctx &C, int slot, const double *host) {
+    const int k = C.sys_of_slot(slot);
+    System &S = *C.sys[k];
+    const int chain = download_i32(C.chain_of)[slot];
+    const int r = chain - S.base;
+    CK(cudaMemcpyAsync(C.stage.p, host, (size_t)S.plan.N * 3 * sizeof(double), cudaMemcpyHostToDevice, C.st));
+    with_args(C, S, [&](auto &a) { launch_scatter(a, r, 1, C.stage.p, C.st); });
+}
+
+static void get_spins_slot(Ctx &C, int slot, double *host) {
+    const int k = C.sys_of_slot(slot);
+    System &S = *C.sys[k];
+    const int chain = download_i32(C.chain_of)[slot];
+    const int r = chain - S.base;
+    with_args(C, S, [&](auto &a) { launch_gather(a, r, 1, C.stage.p, C.st); });
+    CK(cudaMemcpyAsync(host, C.stage.p, (size_t)S.plan.N * 3 * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+}
+
+static bool identity_perm(const std::vector<int32_t> &chain_of, const System &S) {
+    for (int r = 0; r < S.R; r++)
+        if (chain_of[S.base + r] != S.base + r) return false;
+    return true;
+}
+
+static void set_spins_all(Ctx &C, const double *host) {
+    const std::vector<int32_t> chain_of = download_i32(C.chain_of);
+    size_t off = 0;
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        const size_t per = (size_t)S.plan.N * 3;
+        if (identity_perm(chain_of, S)) {
+            CK(cudaMemcpyAsync(C.stage.p, host + off, per * S.R * sizeof(double), cudaMemcpyHostToDevice, C.st));
+            with_args(C, S, [&](auto &a) { launch_scatter(a, 0, S.R, C.stage.p, C.st); });
+        } else {
+            for (int r = 0; r < S.R; r++) {
+                CK(cudaMemcpyAsync(C.stage.p, host + off + r * per, per * sizeof(double), cudaMemcpyHostToDevice,
+                                   C.st));
+                const int cr = chain_of[S.base + r] - S.base;
+                with_args(C, S, [&](auto &a) { launch_scatter(a, cr, 1, C.stage.p, C.st); });
+            }
+        }
+        off += per * S.R;
+    }
+}
+
+static void get_spins_all(Ctx &C, double *host) {
+    const std::vector<int32_t> chain_of = download_i32(C.chain_of);
+    size_t off = 0;
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        const size_t per = (size_t)S.plan.N * 3;
+        if (identity_perm(chain_of, S)) {
+            with_args(C, S, [&](auto &a) { launch_gather(a, 0, S.R, C.stage.p, C.st); });
+            CK(cudaMemcpyAsync(host + off, C.stage.p, per * S.R * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+        } else {
+            for (int r = 0; r < S.R; r++) {
+                const int cr = chain_of[S.base + r] - S.base;
+                with_args(C, S, [&](auto &a) { launch_gather(a, cr, 1, C.stage.p, C.st); });
+                CK(cudaMemcpyAsync(host + off + r * per, C.stage.p, per * sizeof(double), cudaMemcpyDeviceToHost,
+                                   C.st));
+            }
+        }
+        off += per * S.R;
+    }
+}
+
+// chain-indexed device values -> slot-indexed host values
+static void chain_to_slot(Ctx &C, const DevBuf<double> &v, double *out) {
+    const std::vector<double> x = download_f64(v, C.n_chains);
+    const std::vector<int32_t> slot_of = download_i32(C.slot_of);
+    for (int c = 0; c < C.n_chains; c++) out[slot_of[c]] = x[c];
+}
+
+// ------------------------------------------------------------ sweeps (global path)
+
+struct Launches {
+    int64_t n = 0;
+};
+
+// One sweep of `what` (0 OR, 1 Metropolis, 2 deterministic) over all replicas
+// of every lattice; per_replica issues one launch per replica per class.
+static void sweep_global(Ctx &C, int what, int kind, double T_override, bool per_replica, Launches &L) {
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        const Plan &P = S.plan;
+        with_args(C, S, [&](auto &a) {
+            for (int col = 0; col < P.n_colours; col++) {
+                const int64_t st = P.col_start[col], n = P.col_count[col];
+                const int groups = per_replica ? S.R : 1;
+                for (int g = 0; g < groups; g++) {
+                    const int lo = per_replica ? g : 0, cnt = per_replica ? 1 : S.R;
+                    if (what == 0) launch_or_colour(a, st, n, lo, cnt, C.st);
+                    else if (what == 1) launch_metro_colour(a, C.cs, st, n, lo, cnt, kind, C.msweep, T_override, C.st);
+                    else launch_det_colour(a, st, n, lo, cnt, C.st);
+                    L.n++;
+                }
+            }
+        });
+        if (what == 1) {
+            launch_after_metro(C.cs, S.base, S.R, kind, P.N, C.last_acc.p, C.st);
+            L.n++;
+        }
+    }
+    if (what == 1) C.msweep++;
+}
+
+static void energy_all(Ctx &C, Launches &L) {
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        with_args(C, S, [&](auto &a) { launch_energy(a, C.cs, 0, S.R, C.part.p, C.st); });
+        L.n += 2;
+    }
+}
+static void magnet_all(Ctx &C, Launches &L) {
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        with_args(C, S, [&](auto &a) { launch_magnet(a, C.cs, 0, S.R, C.part.p, C.st); });
+        L.n += 2;
+    }
+}
+static void renorm_all(Ctx &C, Launches &L) {
+    if (C.precision != CSMC_FP32) return;
+    for (auto &Sp : C.sys) {
+        launch_renorm(Sp->fa, 0, Sp->R, C.st);
+        L.n++;
+    }
+}
+
+// ------------------------------------------------------------ run driver
+
+struct Schedule {
+    int64_t start, end; // iterations [start, end)
+    int64_t t_therm;
+    int or_rate, swap_rate, probe_rate, kind;
+    bool swap_enabled;
+    int64_t dosweep;
+    int64_t probe_first, n_probes, cap;
+    bool is_probe(int64_t q) const { return probe_rate > 0 && q >= t_therm && q % probe_rate == 0; }
+    bool is_metro(int64_t q) const { return q % dosweep == 0; }
+    bool is_swap(int64_t q) const { return swap_enabled && is_metro(q) && q % swap_rate == 0; }
+    bool need_E(int64_t it) const {
+        if (is_swap(it)) return true;
+        for (int64_t q = it; q < it + dosweep && q < end; q++)
+            if (is_probe(q)) return true;
+        return it + dosweep >= end;
+    }
+};
+
+static int choose_path(Ctx &C, int requested) {
+    if (requested == CSMC_PATH_GLOBAL || requested == CSMC_PATH_PER_REPLICA) return requested;
+    bool all = true;
+    for (auto &S : C.sys) all = all && S->resident_ok;
+    if (requested == CSMC_PATH_RESIDENT) {
+        require(all, CSMC_ERR_UNSUPPORTED,
+                "resident path needs every replica to fit in shared memory (3 * padded_sites * word size bytes) "
+                "and at most 65536 padded sites");
+        return CSMC_PATH_RESIDENT;
+    }
+    return all ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
+}
+
+static int resident_block(Ctx &C, int hint) {
+    if (hint == 256 || hint == 512 || hint == 1024) return hint;
+    return 512;
+}
+
+static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
+    size_t smem = 0;
+    bool cub = false, qua = false;
+    for (auto &S : C.sys) {
+        smem = std::max(smem, S->resident_smem);
+        cub = cub || S->cub;
+        qua = qua || S->qua;
+    }
+    int per_sm = C.precision == CSMC_FP32 ? resident_max_blocks_per_sm<float>(block, smem, cub, qua)
+                                          : resident_max_blocks_per_sm<double>(block, smem, cub, qua);
+    require(per_sm >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on an SM with this shared memory size");
+    const int grid = std::min(C.n_items, C.n_sms * per_sm);
+    auto ev = C.next_kernel_events();
+    CK(cudaMemsetAsync(C.work_ctr.p, 0, sizeof(int), C.st));
+    CK(cudaEventRecord(ev.first, C.st));
+    cudaError_t e = C.precision == CSMC_FP32
+                        ? launch_resident<float>(C.fres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid, block,
+                                                 smem, cub, qua, C.st)
+                        : launch_resident<double>(C.dres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid,
+                                                  block, smem, cub, qua, C.st);
+    CK(e);
+    CK(cudaEventRecord(ev.second, C.st));
+    L.n += 1;
+}
+
+static void run(Ctx &C, csmc_run_params *p) {
+    require(p != nullptr, CSMC_ERR_INVALID, "params is NULL");
+    require(p->n_sweeps >= 0 && p->sweep_start >= 0, CSMC_ERR_INVALID, "negative sweep range");
+    require(p->overrelaxation_rate >= 0, CSMC_ERR_INVALID, "overrelaxation_rate must be >= 0");
+    require(p->kind >= 0 && p->kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    Schedule s;
+    s.start = p->sweep_start;
+    s.end = p->sweep_start + p->n_sweeps;
+    s.t_therm = p->t_thermalization;
+    s.or_rate = p->overrelaxation_rate;
+    s.swap_rate = p->swap_rate;
+    s.probe_rate = p->probe_rate;
+    s.kind = p->kind;
+    s.dosweep = s.or_rate == 0 ? 1 : s.or_rate;
+    bool any_pt = false;
+    for (auto &S : C.sys) any_pt = any_pt || S->R > 1;
+    s.swap_enabled = s.swap_rate > 0 && any_pt;
+    s.probe_first = 0;
+    s.n_probes = 0;
+    if (s.probe_rate > 0) {
+        int64_t lo = std::max(s.t_therm, s.start);
+        s.probe_first = (lo + s.probe_rate - 1) / s.probe_rate * s.probe_rate;
+        if (s.probe_first < s.end) s.n_probes = (s.end - 1 - s.probe_first) / s.probe_rate + 1;
+    }
+    const bool want_rec = (p->probe_energy || p->probe_magnetization) && s.n_probes > 0;
+    s.cap = want_rec ? std::min<int64_t>(s.n_probes, std::max<int64_t>(p->probe_capacity, 0)) : 0;
+    const int n_slots = C.n_chains;
+    if (s.cap > 0) {
+        if (C.rec_E.n < (size_t)(s.cap * n_slots)) C.rec_E.alloc(s.cap * n_slots);
+        if (C.rec_M.n < (size_t)(s.cap * n_slots)) C.rec_M.alloc(s.cap * n_slots);
+    }
+    double *recE = s.cap > 0 ? C.rec_E.p : nullptr, *recM = s.cap > 0 ? C.rec_M.p : nullptr;
+    C.acc_slot.zero(C.st);
+    C.exch_slot.zero(C.st);
+
+    const int path = choose_path(C, p->path);
+    C.reset_kernel_time();
+    Launches L;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, C.st));
+
+    auto swap_all = [&](int64_t it) {
+        for (size_t k = 0; k < C.sys.size(); k++) {
+            System &S = *C.sys[k];
+            if (S.R < 2) continue;
+            launch_swap(C.cs, S.base, S.R, it, s.swap_rate, (uint32_t)k, C.k0, C.k1, C.st);
+            L.n++;
+        }
+    };
+    auto probe_index = [&](int64_t q) { return (q - s.probe_first) / s.probe_rate; };
+
+    if (path == CSMC_PATH_RESIDENT) {
+        const int block = resident_block(C, p->resident_block);
+        // windows end at exchange iterations; without exchanges, at most
+        // `chunk` iterations per launch
+        const int64_t chunk = 256;
+        int64_t it = s.start;
+        bool pending = false;
+        while (it < s.end) {
+            int64_t to = std::min(s.end, it + chunk) - 1;
+            bool ends_swap = false;
+            if (s.swap_enabled) {
+                for (int64_t q = it; q <= std::min(s.end - 1, it + chunk * std::max(s.swap_rate, 1)); q++)
+                    if (s.is_swap(q)) {
+                        to = q;
+                        ends_swap = true;
+                        break;
+                    }
+                if (!ends_swap) to = s.end - 1;
+            }
+            RunDesc rd{};
+            rd.it0 = it;
+            rd.it1 = to + 1;
+            rd.t_therm = s.t_therm;
+            rd.probe_first = s.probe_first;
+            rd.probe_cap = s.cap;
+            rd.rec_E = recE;
+            rd.rec_M = recM;
+            rd.T_override = 0.0;
+            rd.msweep0 = C.msweep;
+            rd.or_rate = s.or_rate;
+            rd.swap_rate = s.swap_rate;
+            rd.probe_rate = s.probe_rate;
+            rd.kind = s.kind;
+            rd.pending_probe = pending ? 1 : 0;
+            rd.reset_sigma = 0;
+            rd.n_slots = n_slots;
+            rd.renorm_every = C.renorm_every;
+            rd.swap_enabled = s.swap_enabled ? 1 : 0;
+            resident_launch(C, rd, block, L);
+            for (int64_t q = it; q <= to; q++)
+                if (s.is_metro(q)) C.msweep++;
+            pending = false;
+            if (ends_swap) {
+                swap_all(to);
+                pending = s.is_probe(to);
+            }
+            it = to + 1;
+        }
+        if (pending) { // the last exchange iteration was also a probe
+            magnet_all(C, L);
+            for (auto &S : C.sys) {
+                const int64_t kq = probe_index(s.end - 1);
+                if (kq < s.cap) launch_probe_record(C.cs, S->base, S->R, recE, recM, kq, n_slots, C.st);
+                L.n++;
+            }
+        }
+    } else {
+        const bool per_rep = path == CSMC_PATH_PER_REPLICA;
+        int since_renorm = 0;
+        for (int64_t it = s.start; it < s.end; it++) {
+            if (s.or_rate != 0) {
+                sweep_global(C, 0, 0, 0.0, per_rep, L);
+                since_renorm++;
+            }
+            if (s.is_metro(it)) {
+                sweep_global(C, 1, s.kind, 0.0, per_rep, L);
+                since_renorm++;
+                if (s.need_E(it)) energy_all(C, L);
+                if (s.is_swap(it)) swap_all(it);
+            }
+            if (s.is_probe(it)) {
+                magnet_all(C, L);
+                const int64_t kq = probe_index(it);
+                if (kq < s.cap)
+                    for (auto &S : C.sys) {
+                        launch_probe_record(C.cs, S->base, S->R, recE, recM, kq, n_slots, C.st);
+                        L.n++;
+                    }
+            }
+            if (C.renorm_every > 0 && since_renorm >= C.renorm_every) {
+                renorm_all(C, L);
+                since_renorm = 0;
+            }
+        }
+        if (since_renorm > 0 && C.renorm_every > 0) renorm_all(C, L);
+    }
+    CK(cudaEventRecord(e1, C.st));
+    sync_check(C);
+    C.collect_kernel_time();
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    C.last_ms = ms;
+    C.last_launches = L.n;
+
+    if (s.cap > 0) {
+        const size_t n = (size_t)s.cap * n_slots;
+        if (p->probe_energy) CK(cudaMemcpy(p->probe_energy, C.rec_E.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (p->probe_magnetization)
+            CK(cudaMemcpy(p->probe_magnetization, C.rec_M.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    if (p->accepted) {
+        std::vector<double> a = download_f64(C.acc_slot, n_slots);
+        for (int q = 0; q < n_slots; q++) p->accepted[q] += a[q];
+    }
+    if (p->exchanged) {
+        std::vector<double> a = download_f64(C.exch_slot, n_slots);
+        for (int q = 0; q < n_slots; q++) p->exchanged[q] += a[q];
+    }
+    p->n_probes_out = s.cap;
+}
+
+static void anneal(Ctx &C, const double *temps, int n_temps, int64_t t_therm, int or_rate, int kind, double sigma0,
+                   int path_req, double *accepted) {
+    require(n_temps >= 0 && (n_temps == 0 || temps), CSMC_ERR_INVALID, "temperatures missing");
+    require(or_rate >= 0, CSMC_ERR_INVALID, "overrelaxation_rate must be >= 0");
+    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    const int path = choose_path(C, path_req);
+    C.reset_kernel_time();
+    const int n_slots = C.n_chains;
+    Launches L;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float total_ms = 0.f;
+    const int64_t dosweep = or_rate == 0 ? 1 : or_rate;
+    for (int k = 0; k < n_temps; k++) {
+        const double T = temps[k];
+        require(T > 0, CSMC_ERR_INVALID, "temperatures must be > 0");
+        C.acc_slot.zero(C.st);
+        CK(cudaEventRecord(e0, C.st));
+        if (t_therm > 1) {
+            if (path == CSMC_PATH_RESIDENT) {
+                RunDesc rd{};
+                rd.it0 = 1; // t = 1 .. t_thermalization-1 (monte_carlo.jl:169-182)
+                rd.it1 = t_therm;
+                rd.t_therm = INT64_MAX;
+                rd.T_override = T;
+                rd.sigma0 = sigma0;
+                rd.msweep0 = C.msweep;
+                rd.or_rate = or_rate;
+                rd.swap_rate = 0;
+                rd.probe_rate = 0;
+                rd.kind = kind;
+                rd.reset_sigma = 1;
+                rd.n_slots = n_slots;
+                rd.renorm_every = C.renorm_every;
+                resident_launch(C, rd, resident_block(C, 0), L);
+                for (int64_t t = 1; t < t_therm; t++)
+                    if (t % dosweep == 0) C.msweep++;
+            } else {
+                std::vector<double> sg(n_slots, sigma0);
+                CK(cudaMemcpyAsync(C.sigma_slot.p, sg.data(), n_slots * sizeof(double), cudaMemcpyHostToDevice, C.st));
+                CK(cudaStreamSynchronize(C.st));
+                const bool per_rep = path == CSMC_PATH_PER_REPLICA;
+                int since = 0;
+                for (int64_t t = 1; t < t_therm; t++) {
+                    if (or_rate != 0) {
+                        sweep_global(C, 0, 0, T, per_rep, L);
+                        since++;
+                    }
+                    if (t % dosweep == 0) {
+                        sweep_global(C, 1, kind, T, per_rep, L);
+                        since++;
+                    }
+                    if (C.renorm_every > 0 && since >= C.renorm_every) {
+                        renorm_all(C, L);
+                        since = 0;
+                    }
+                }
+                if (since > 0 && C.renorm_every > 0) renorm_all(C, L);
+            }
+        }
+        CK(cudaEventRecord(e1, C.st));
+        sync_check(C);
+        C.collect_kernel_time();
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        total_ms += ms;
+        if (accepted) {
+            std::vector<double> a = download_f64(C.acc_slot, n_slots);
+            std::copy(a.begin(), a.end(), accepted + (size_t)k * n_slots);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    C.last_ms = total_ms;
+    C.last_launches = L.n;
+}
+
+static void ensure_exact(Ctx &C, System &S) {
+    if (S.exact_ready) return;
+    const Plan &P = S.plan;
+    const int64_t N = P.N;
+    std::vector<int64_t> bs(N * P.N2 + 1), cs(N * P.N3 * 2 + 1), qs(N * P.N4 * 3 + 1);
+    std::vector<double> bm(N * P.N2 * 9 + 1), ct(N * P.N3 * 27 + 1), qt(N * P.N4 * 81 + 1), f(N * 3), o(N * 9);
+    export_tables(P, bs.data(), bm.data(), cs.data(), ct.data(), qs.data(), qt.data(), f.data(), o.data());
+    for (auto &v : bs) v -= 1;
+    for (auto &v : cs) v -= 1;
+    for (auto &v : qs) v -= 1;
+    S.xbs.upload(bs);
+    S.xcs.upload(cs);
+    S.xqs.upload(qs);
+    S.xbm.upload(bm);
+    S.xct.upload(ct);
+    S.xqt.upload(qt);
+    S.xfield.upload(f);
+    S.xonsite.upload(o);
+    S.exact_ready = true;
+}
+
+} // namespace csmc
+
+using namespace csmc;
+
+#define API_BEGIN try {
+#define API_END                                                                                                        \
+    }                                                                                                                  \
+    catch (const Error &e) {                                                                                           \
+        g_err = e.what();                                                                                              \
+        return e.code;                                                                                                 \
+    }                                                                                                                  \
+    catch (const std::bad_alloc &) {                                                                                   \
+        g_err = "host allocation failed";                                                                              \
+        return CSMC_ERR_OOM;                                                                                           \
+    }                                                                                                                  \
+    catch (const std::exception &e) {                                                                                  \
+        g_err = e.what();                                                                                              \
+        return CSMC_ERR_INVALID;                                                                                       \
+    }                                                                                                                  \
+    return CSMC_OK;
+
+static Ctx &ctx_of(void *c) {
+    require(c != nullptr, CSMC_ERR_INVALID, "context is NULL");
+    return *static_cast<Ctx *>(c);
+}
+
+extern "C" {
+
+const char *csmc_last_error(void) { return g_err.c_str(); }
+const char *csmc_version(void) { return "csmc 0.1 sm_103a"; }
+
+int csmc_lattice_plan(const csmc_lattice_desc *desc, csmc_lattice_info *info) {
+    API_BEGIN
+    require(info != nullptr, CSMC_ERR_INVALID, "info is NULL");
+    Plan p = make_plan(desc);
+    fill_info(p, info);
+    API_END
+}
+
+int csmc_lattice_tables(const csmc_lattice_desc *desc, int64_t *bs, double *bm, int64_t *cs, double *ct, int64_t *qs,
+                        double *qt, double *field, double *onsite) {
+    API_BEGIN
+    Plan p = make_plan(desc);
+    export_tables(p, bs, bm, cs, ct, qs, qt, field, onsite);
+    API_END
+}
+
+int csmc_lattice_colouring(const csmc_lattice_desc *desc, int32_t *colour_of_site, int64_t *ref_of_device,
+                           int64_t *colour_start) {
+    API_BEGIN
+    Plan p = make_plan(desc);
+    if (colour_of_site) std::copy(p.colour_of.begin(), p.colour_of.end(), colour_of_site);
+    if (ref_of_device) std::copy(p.dev2ref.begin(), p.dev2ref.end(), ref_of_device);
+    if (colour_start) std::copy(p.col_start.begin(), p.col_start.end(), colour_start);
+    API_END
+}
+
+int csmc_create(const csmc_lattice_desc *desc, int32_t precision, int32_t n_replicas, uint64_t seed, void **out) {
+    API_BEGIN
+    require(out != nullptr, CSMC_ERR_INVALID, "ctx_out is NULL");
+    *out = nullptr;
+    *out = create(desc, 1, &n_replicas, precision, seed);
+    API_END
+}
+
+int csmc_create_batch(const csmc_lattice_desc *descs, int32_t n, const int32_t *reps, int32_t precision, uint64_t seed,
+                      void **out) {
+    API_BEGIN
+    require(out != nullptr && descs != nullptr && reps != nullptr, CSMC_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    *out = create(descs, n, reps, precision, seed);
+    API_END
+}
+
+int csmc_destroy(void *c) {
+    API_BEGIN
+    if (c) {
+        Ctx *C = static_cast<Ctx *>(c);
+        cudaStreamSynchronize(C->st);
+        delete C;
+    }
+    API_END
+}
+
+int csmc_num_slots(void *c, int32_t *n) {
+    API_BEGIN
+    require(n != nullptr, CSMC_ERR_INVALID, "n_slots is NULL");
+    *n = ctx_of(c).n_chains;
+    API_END
+}
+
+int csmc_lattice_info_of(void *c, int32_t k, csmc_lattice_info *info) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(k >= 0 && k < (int)C.sys.size() && info, CSMC_ERR_INVALID, "bad lattice index");
+    fill_info(C.sys[k]->plan, info);
+    API_END
+}
+
+int csmc_set_spins(void *c, int32_t slot, const double *spins) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
+    set_spins_slot(C, slot, spins);
+    sync_check(C);
+    API_END
+}
+
+int csmc_get_spins(void *c, int32_t slot, double *spins) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
+    get_spins_slot(C, slot, spins);
+    sync_check(C);
+    API_END
+}
+
+int csmc_set_spins_all(void *c, const double *spins) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
+    set_spins_all(C, spins);
+    sync_check(C);
+    API_END
+}
+
+int csmc_get_spins_all(void *c, double *spins) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
+    get_spins_all(C, spins);
+    sync_check(C);
+    API_END
+}
+
+int csmc_random_spins(void *c, uint64_t seed) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    for (auto &S : C.sys) with_args(C, *S, [&](auto &a) { launch_random_spins(a, (uint32_t)seed, (uint32_t)(seed >> 32), C.st); });
+    sync_check(C);
+    API_END
+}
+
+int csmc_set_temperatures(void *c, const double *T) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(T != nullptr, CSMC_ERR_INVALID, "T is NULL");
+    for (int k = 0; k < C.n_chains; k++) require(T[k] > 0, CSMC_ERR_INVALID, "temperatures must be > 0");
+    CK(cudaMemcpy(C.T_slot.p, T, C.n_chains * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<int32_t> ident(C.n_chains);
+    std::iota(ident.begin(), ident.end(), 0);
+    CK(cudaMemcpy(C.slot_of.p, ident.data(), ident.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(C.chain_of.p, ident.data(), ident.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    API_END
+}
+
+int csmc_set_sigma(void *c, const double *sigma) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(sigma != nullptr, CSMC_ERR_INVALID, "sigma is NULL");
+    CK(cudaMemcpy(C.sigma_slot.p, sigma, C.n_chains * sizeof(double), cudaMemcpyHostToDevice));
+    API_END
+}
+
+int csmc_get_sigma(void *c, double *sigma) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(sigma != nullptr, CSMC_ERR_INVALID, "sigma is NULL");
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaMemcpy(sigma, C.sigma_slot.p, C.n_chains * sizeof(double), cudaMemcpyDeviceToHost));
+    API_END
+}
+
+int csmc_get_permutation(void *c, int32_t *replica_of_slot) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(replica_of_slot != nullptr, CSMC_ERR_INVALID, "output is NULL");
+    CK(cudaStreamSynchronize(C.st));
+    std::vector<int32_t> v = download_i32(C.chain_of);
+    std::copy(v.begin(), v.end(), replica_of_slot);
+    API_END
+}
+
+int csmc_local_field(void *c, int32_t slot, double *H) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(H != nullptr, CSMC_ERR_INVALID, "H is NULL");
+    System &S = *C.sys[C.sys_of_slot(slot)];
+    const int r = download_i32(C.chain_of)[slot] - S.base;
+    with_args(C, S, [&](auto &a) { launch_local_field(a, r, C.stage.p, C.st); });
+    CK(cudaMemcpyAsync(H, C.stage.p, S.plan.N * 3 * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    sync_check(C);
+    API_END
+}
+
+int csmc_energy_diff(void *c, int32_t slot, int64_t n, const int64_t *sites, const double *ns, double *dE) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(n >= 0 && (n == 0 || (sites && ns && dE)), CSMC_ERR_INVALID, "NULL argument");
+    System &S = *C.sys[C.sys_of_slot(slot)];
+    for (int64_t q = 0; q < n; q++)
+        require(sites[q] >= 0 && sites[q] < S.plan.N, CSMC_ERR_INVALID, "site index out of range");
+    const int r = download_i32(C.chain_of)[slot] - S.base;
+    DevBuf<int64_t> ds;
+    DevBuf<double> dn, de;
+    ds.upload(sites, n);
+    dn.upload(ns, 3 * n);
+    de.alloc(n);
+    with_args(C, S, [&](auto &a) { launch_energy_diff(a, r, n, ds.p, dn.p, de.p, C.st); });
+    sync_check(C);
+    if (n) CK(cudaMemcpy(dE, de.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    API_END
+}
+
+int csmc_total_energy(void *c, double *E) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(E != nullptr, CSMC_ERR_INVALID, "E is NULL");
+    Launches L;
+    energy_all(C, L);
+    sync_check(C);
+    chain_to_slot(C, C.E_chain, E);
+    API_END
+}
+
+int csmc_magnetization(void *c, double *M) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(M != nullptr, CSMC_ERR_INVALID, "M is NULL");
+    Launches L;
+    magnet_all(C, L);
+    sync_check(C);
+    chain_to_slot(C, C.M_chain, M);
+    API_END
+}
+
+int csmc_metropolis_sweep(void *c, int32_t kind, double *accepted) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    Launches L;
+    sweep_global(C, 1, kind, 0.0, false, L);
+    sync_check(C);
+    if (accepted) {
+        std::vector<double> a = download_f64(C.last_acc, C.n_chains);
+        std::copy(a.begin(), a.end(), accepted);
+    }
+    API_END
+}
+
+int csmc_overrelax_sweep(void *c) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    Launches L;
+    sweep_global(C, 0, 0, 0.0, false, L);
+    sync_check(C);
+    API_END
+}
+
+int csmc_deterministic_sweeps(void *c, int64_t n) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(n >= 0, CSMC_ERR_INVALID, "n_sweeps must be >= 0");
+    Launches L;
+    for (int64_t k = 0; k < n; k++) sweep_global(C, 2, 0, 0.0, false, L);
+    sync_check(C);
+    API_END
+}
+
+int csmc_replay(void *c, int32_t slot, int32_t kind, double T, double *sigma, int64_t n, const int64_t *sites,
+                const double *u_phi, const double *u_z, const double *u_acc, uint8_t *accepted) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(C.precision == CSMC_FP64, CSMC_ERR_UNSUPPORTED, "replay needs a CSMC_FP64 context");
+    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(n >= 0 && (n == 0 || (sites && u_phi && u_z && u_acc && accepted)), CSMC_ERR_INVALID, "NULL argument");
+    require(T > 0, CSMC_ERR_INVALID, "T must be > 0");
+    System &S = *C.sys[C.sys_of_slot(slot)];
+    for (int64_t q = 0; q < n; q++)
+        require(sites[q] >= 0 && sites[q] < S.plan.N, CSMC_ERR_INVALID, "site index out of range");
+    ensure_exact(C, S);
+    const int r = download_i32(C.chain_of)[slot] - S.base;
+    DevBuf<int64_t> ds;
+    DevBuf<double> dp, dz, da, dsig;
+    DevBuf<uint8_t> dacc;
+    ds.upload(sites, n);
+    dp.upload(u_phi, n);
+    dz.upload(u_z, n);
+    da.upload(u_acc, n);
+    double sg = sigma ? *sigma : 60.0;
+    dsig.upload(&sg, 1);
+    dacc.alloc(n);
+    ExactTables t{};
+    t.N = S.plan.N;
+    t.N2 = S.plan.N2;
+    t.N3 = S.plan.N3;
+    t.N4 = S.plan.N4;
+    t.bs = S.xbs.p;
+    t.cs = S.xcs.p;
+    t.qs = S.xqs.p;
+    t.bm = S.xbm.p;
+    t.ct = S.xct.p;
+    t.qt = S.xqt.p;
+    t.field = S.xfield.p;
+    t.onsite = S.xonsite.p;
+    t.ref2dev = S.ref2dev.p;
+    t.Np = S.plan.Np;
+    t.S = S.plan.desc.S;
+    if (n > 0)
+        launch_replay(t, S.dspins.p + (size_t)r * 3 * S.plan.Np, kind, T, dsig.p, n, ds.p, dp.p, dz.p, da.p, dacc.p,
+                      C.st);
+    sync_check(C);
+    if (n) CK(cudaMemcpy(accepted, dacc.p, n, cudaMemcpyDeviceToHost));
+    if (sigma) CK(cudaMemcpy(sigma, dsig.p, sizeof(double), cudaMemcpyDeviceToHost));
+    API_END
+}
+
+int csmc_run(void *c, csmc_run_params *p) {
+    API_BEGIN
+    run(ctx_of(c), p);
+    API_END
+}
+
+int csmc_anneal(void *c, const double *temps, int32_t n_temps, int64_t t_therm, int32_t or_rate, int32_t kind,
+                double sigma0, int32_t path, double *accepted) {
+    API_BEGIN
+    anneal(ctx_of(c), temps, n_temps, t_therm, or_rate, kind, sigma0, path, accepted);
+    API_END
+}
+
+int csmc_set_renormalize(void *c, int32_t every) {
+    API_BEGIN
+    require(every >= 0, CSMC_ERR_INVALID, "interval must be >= 0");
+    ctx_of(c).renorm_every = every;
+    API_END
+}
+
+int csmc_spin_length_drift(void *c, double *drift) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(drift != nullptr, CSMC_ERR_INVALID, "drift is NULL");
+    C.drift_bits.zero(C.st);
+    for (auto &S : C.sys) with_args(C, *S, [&](auto &a) { launch_drift(a, C.drift_bits.p, C.st); });
+    sync_check(C);
+    unsigned int bits = 0;
+    CK(cudaMemcpy(&bits, C.drift_bits.p, sizeof(bits), cudaMemcpyDeviceToHost));
+    float f;
+    std::memcpy(&f, &bits, sizeof(f));
+    *drift = f;
+    API_END
+}
+
+int csmc_last_run_stats(void *c, double *ms, int64_t *launches, double *sweep_kernel_ms,
+                        int64_t *sweep_kernel_launches) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    if (ms) *ms = C.last_ms;
+    if (launches) *launches = C.last_launches;
+    if (sweep_kernel_ms) *sweep_kernel_ms = C.last_kernel_ms;
+    if (sweep_kernel_launches) *sweep_kernel_launches = C.last_kernel_launches;
+    API_END
+}
+
+} // extern "C"

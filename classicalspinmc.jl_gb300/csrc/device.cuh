@@ -1,0 +1,242 @@
+// device.cuh -- device-side data views and per-site physics shared by the
+// colour-sweep kernels (kernels.cu) and the replay kernel (exact.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/csmc.h"
+
+namespace csmc {
+
+// Philox stream purposes (counter word 3); the oracle uses the same values.
+enum : uint32_t { PURPOSE_METRO_A = 1, PURPOSE_METRO_B = 2, PURPOSE_SWAP = 3, PURPOSE_INIT = 4 };
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the
+// multiply-xor S-box with Weyl key schedule.
+struct U4 {
+    uint32_t x, y, z, w;
+};
+__host__ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                     uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+__host__ __device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+__host__ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    return (double)m * (1.0 / 9007199254740992.0);
+}
+
+// One lattice ("system") as the kernels see it.  Idx is the partner index
+// type: uint32 for the global path, uint16 for shared-memory residents.
+template <typename Idx> struct Tab {
+    const Idx *p2, *p3, *p4; // [W][k][Np]
+    const uint8_t *pat;      // basis (pattern) of each device site
+    int64_t Np;
+    int W2, W3, W4;
+};
+
+// Coupling coefficients in the arithmetic type R; pattern b = basis, nb =
+// padding.  Pointers may point to global or shared memory.
+template <typename R> struct Coef {
+    const R *mats, *cubs, *quas; // deduplicated tensors, id 0 = zeros
+    const R *O, *P, *h;          // per pattern: onsite (9), folded self loops (9), field (3)
+    const int32_t *c2, *c3, *c4; // per pattern x slot: coefficient ids
+};
+
+template <typename R> struct V3 {
+    R x, y, z;
+};
+
+// Fields on site d from its partners, split by term order, without onsite,
+// self loops or the Zeeman field:
+//   hb = sum_n J_n s_j (bilinear), hc_a = sum C[a,b,c] s_j,b s_k,c,
+//   hq_a = sum R[a,b,c,d] s_j,b s_k,c s_l,d  (hamiltonian.jl:24-65).
+template <typename R, typename Idx, bool CUB, bool QUA>
+__device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R> &cf, const R *__restrict__ x,
+                                               const R *__restrict__ y, const R *__restrict__ z, int64_t d, int b,
+                                               V3<R> &hb, V3<R> &hc, V3<R> &hq) {
+    hb = {R(0), R(0), R(0)};
+    hc = {R(0), R(0), R(0)};
+    hq = {R(0), R(0), R(0)};
+    const int64_t Np = tb.Np;
+    for (int t = 0; t < tb.W2; t++) {
+        const int64_t j = tb.p2[t * Np + d];
+        const R *M = cf.mats + 9 * cf.c2[b * tb.W2 + t];
+        const R sx = x[j], sy = y[j], sz = z[j];
+        hb.x += M[0] * sx + M[1] * sy + M[2] * sz;
+        hb.y += M[3] * sx + M[4] * sy + M[5] * sz;
+        hb.z += M[6] * sx + M[7] * sy + M[8] * sz;
+    }
+    if (CUB) {
+        for (int t = 0; t < tb.W3; t++) {
+            const int64_t j = tb.p3[(2 * t) * Np + d], k = tb.p3[(2 * t + 1) * Np + d];
+            const R *C = cf.cubs + 27 * cf.c3[b * tb.W3 + t];
+            const R a0 = x[j], a1 = y[j], a2 = z[j], b0 = x[k], b1 = y[k], b2 = z[k];
+            R o[9] = {a0 * b0, a0 * b1, a0 * b2, a1 * b0, a1 * b1, a1 * b2, a2 * b0, a2 * b1, a2 * b2};
+            R sx = 0, sy = 0, sz = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+                sx += C[q] * o[q];
+                sy += C[9 + q] * o[q];
+                sz += C[18 + q] * o[q];
+            }
+            hc.x += sx;
+            hc.y += sy;
+            hc.z += sz;
+        }
+    }
+    if (QUA) {
+        for (int t = 0; t < tb.W4; t++) {
+            const int64_t j = tb.p4[(3 * t) * Np + d], k = tb.p4[(3 * t + 1) * Np + d], l = tb.p4[(3 * t + 2) * Np + d];
+            const R *Q = cf.quas + 81 * cf.c4[b * tb.W4 + t];
+            const R a[3] = {x[j], y[j], z[j]}, bb[3] = {x[k], y[k], z[k]}, c[3] = {x[l], y[l], z[l]};
+            R sx = 0, sy = 0, sz = 0;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const R ab = a[p] * bb[q];
+#pragma unroll
+                    for (int r = 0; r < 3; r++) {
+                        const R o = ab * c[r];
+                        const int idx = (p * 3 + q) * 3 + r;
+                        sx += Q[idx] * o;
+                        sy += Q[27 + idx] * o;
+                        sz += Q[54 + idx] * o;
+                    }
+                }
+            hq.x += sx;
+            hq.y += sy;
+            hq.z += sz;
+        }
+    }
+}
+
+template <typename R> __device__ __forceinline__ V3<R> matvec(const R *M, V3<R> s) {
+    return {M[0] * s.x + M[1] * s.y + M[2] * s.z, M[3] * s.x + M[4] * s.y + M[5] * s.z,
+            M[6] * s.x + M[7] * s.y + M[8] * s.z};
+}
+template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// get_local_field (hamiltonian.jl:3-67): 2 O s + (self loops) + partners - h.
+template <typename R, typename Idx, bool CUB, bool QUA>
+__device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const R *x, const R *y,
+                                             const R *z, int64_t d, int b) {
+    V3<R> hb, hc, hq;
+    partner_fields<R, Idx, CUB, QUA>(tb, cf, x, y, z, d, b, hb, hc, hq);
+    const V3<R> s = {x[d], y[d], z[d]};
+    const V3<R> os = matvec(cf.O + 9 * b, s), ps = matvec(cf.P + 9 * b, s);
+    const R *h = cf.h + 3 * b;
+    return {R(2) * os.x + ps.x + hb.x + hc.x + hq.x - h[0], R(2) * os.y + ps.y + hb.y + hc.y + hq.y - h[1],
+            R(2) * os.z + ps.z + hb.z + hc.z + hq.z - h[2]};
+}
+
+// Energy of moving site d from s to sn with all other spins fixed:
+// e(s) = s.(O+P).s + s.(hb + hc + hq - h)  (hamiltonian.jl:139-196), so
+// dE = sn.Q.sn - s.Q.s + (sn - s).hext.
+template <typename R>
+__device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn, V3<R> hext) {
+    const R *O = cf.O + 9 * b, *P = cf.P + 9 * b;
+    R q[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) q[k] = O[k] + P[k];
+    const R en = dot(sn, matvec(q, sn)), eo = dot(s, matvec(q, s));
+    const V3<R> ds = {sn.x - s.x, sn.y - s.y, sn.z - s.z};
+    return (en - eo) + dot(ds, hext);
+}
+
+// Contribution of site d to total_energy (hamiltonian.jl:70-132):
+// -s.h + s.O.s + (s.hb + s.P.s)/2 + s.hc/3 + s.hq/4.
+template <typename R, typename Idx, bool CUB, bool QUA>
+__device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const R *x, const R *y,
+                                                    const R *z, int64_t d, int b) {
+    V3<R> hb, hc, hq;
+    partner_fields<R, Idx, CUB, QUA>(tb, cf, x, y, z, d, b, hb, hc, hq);
+    const V3<R> s = {x[d], y[d], z[d]};
+    const R *h = cf.h + 3 * b;
+    const R eo = dot(s, matvec(cf.O + 9 * b, s));
+    const R ep = dot(s, matvec(cf.P + 9 * b, s));
+    const R ez = s.x * h[0] + s.y * h[1] + s.z * h[2];
+    double e = -(double)ez + (double)eo + 0.5 * ((double)dot(s, hb) + (double)ep);
+    if (CUB) e += (double)dot(s, hc) / 3.0;
+    if (QUA) e += 0.25 * (double)dot(s, hq);
+    return e;
+}
+
+template <typename R> struct Math;
+template <> struct Math<float> {
+    static __device__ __forceinline__ void sincospi2(float u, float *s, float *c) { sincospif(2.0f * u, s, c); }
+    static __device__ __forceinline__ float sqrt_(float v) { return sqrtf(v); }
+    static __device__ __forceinline__ float rsqrt_(float v) { return rsqrtf(v); }
+    static __device__ __forceinline__ float exp_(float v) { return __expf(v); }
+};
+template <> struct Math<double> {
+    static __device__ __forceinline__ void sincospi2(double u, double *s, double *c) { sincospi(2.0 * u, s, c); }
+    static __device__ __forceinline__ double sqrt_(double v) { return sqrt(v); }
+    static __device__ __forceinline__ double rsqrt_(double v) { return rsqrt(v); }
+    static __device__ __forceinline__ double exp_(double v) { return exp(v); }
+};
+
+// Uniforms of one Metropolis proposal from the Philox stream keyed by the
+// context seed; counter = (device site, Metropolis sweep, replica, purpose).
+template <typename R> struct Draw;
+template <> struct Draw<float> {
+    float uphi, uz, uacc;
+    __device__ __forceinline__ Draw(uint32_t d, uint32_t sweep, uint32_t chain, uint32_t k0, uint32_t k1) {
+        U4 w = philox4x32_10(d, sweep, chain, PURPOSE_METRO_A, k0, k1);
+        uphi = u24(w.x);
+        uz = u24(w.y);
+        uacc = u24(w.z);
+    }
+    __device__ __forceinline__ float acc(uint32_t, uint32_t, uint32_t, uint32_t, uint32_t) const { return uacc; }
+};
+template <> struct Draw<double> {
+    double uphi, uz;
+    __device__ __forceinline__ Draw(uint32_t d, uint32_t sweep, uint32_t chain, uint32_t k0, uint32_t k1) {
+        U4 w = philox4x32_10(d, sweep, chain, PURPOSE_METRO_A, k0, k1);
+        uphi = u53(w.x, w.y);
+        uz = u53(w.z, w.w);
+    }
+    __device__ __forceinline__ double acc(uint32_t d, uint32_t sweep, uint32_t chain, uint32_t k0, uint32_t k1) const {
+        U4 w = philox4x32_10(d, sweep, chain, PURPOSE_METRO_B, k0, k1);
+        return u53(w.x, w.y);
+    }
+};
+
+// random_spin_orientation (lattice.jl:306-311) and gaussian_move
+// (metropolis.jl:84-87) for uniforms (uphi, uz).
+template <typename R>
+__device__ __forceinline__ V3<R> propose(int kind, R S, R sigma, V3<R> s, R uphi, R uz) {
+    R sp, cp;
+    Math<R>::sincospi2(uphi, &sp, &cp);
+    const R zz = R(2) * uz - R(1);
+    R r2 = R(1) - zz * zz;
+    const R r = Math<R>::sqrt_(r2 > R(0) ? r2 : R(0));
+    V3<R> u = {S * (r * cp), S * (r * sp), S * zz};
+    if (kind == CSMC_METROPOLIS) return u;
+    V3<R> v = {s.x + sigma * u.x, s.y + sigma * u.y, s.z + sigma * u.z};
+    const R inv = S * Math<R>::rsqrt_(v.x * v.x + v.y * v.y + v.z * v.z);
+    return {v.x * inv, v.y * inv, v.z * inv};
+}
+
+} // namespace csmc

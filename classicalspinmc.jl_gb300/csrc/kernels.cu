@@ -1,0 +1,787 @@
+// kernels.cu -- sm_103a colour-sweep kernels for the Metropolis /
+// overrelaxation / deterministic updates, the energy and magnetisation
+// reductions and the replica exchange, in two execution forms:
+//
+//  * global path: one launch per colour class, all replicas of a lattice in
+//    the grid's y dimension (or one replica per launch for the plain path);
+//    spins live in HBM/L2, partner tables are 32-bit.
+//  * resident path: a persistent kernel, one CTA per replica, that stages
+//    the replica into shared memory with bulk TMA copies (cp.async.bulk,
+//    mbarrier completion), runs a whole window of sweeps there with
+//    __syncthreads between colour classes, and writes it back once.
+//
+// The physics per site restates hamiltonian.jl, metropolis.jl and
+// monte_carlo.jl (see device.cuh).  Colour classes make every update within
+// a class independent, so each class is one parallel step.
+#include "kernels.cuh"
+#include "launch.hpp"
+
+namespace csmc {
+
+constexpr int GB = 256; // block size of the global-path kernels
+
+// ------------------------------------------------------------ reductions
+
+template <int NT> __device__ __forceinline__ double block_sum(double v, double *scratch) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) scratch[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < NT / 32 ? scratch[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t; // valid in thread 0
+}
+
+__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------ global path
+
+template <typename R> struct Ptrs {
+    R *x, *y, *z;
+};
+template <typename R> __device__ __forceinline__ Ptrs<R> replica(const SysArgs<R> &a, int r) {
+    R *x = a.spins + (int64_t)r * 3 * a.tb.Np;
+    return {x, x + a.tb.Np, x + 2 * a.tb.Np};
+}
+
+// One Metropolis colour step: every site of the class proposes once
+// (metropolis.jl:65-82, with site order given by the colouring).
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs, int64_t start, int64_t count,
+                                                     int chain_lo, int kind, uint32_t msweep, double T_override) {
+    const int r = chain_lo + blockIdx.y;
+    const int c = a.chain_base + r;
+    const Ptrs<R> p = replica(a, r);
+    const int slot = cs.slot_of[c];
+    const double T = T_override > 0 ? T_override : cs.T_slot[slot];
+    const R sigma = (R)cs.sigma_slot[slot];
+    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    unsigned acc = 0;
+    if (i < count) {
+        const int64_t d = start + i;
+        const int b = a.tb.pat[d];
+        V3<R> hb, hc, hq;
+        partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b, hb, hc, hq);
+        const R *h = a.cf.h + 3 * b;
+        const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+        const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+        const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1);
+        const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
+        const R dE = delta_e<R>(a.cf, b, s, sn, hext);
+        bool accept = dE < R(0);
+        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(-dE / (R)T);
+        if (accept) {
+            p.x[d] = sn.x;
+            p.y[d] = sn.y;
+            p.z[d] = sn.z;
+            acc = 1;
+        }
+    }
+    acc = warp_sum_u(acc);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&cs.sweep_acc[c], (unsigned long long)acc);
+}
+
+// overrelaxation! body (monte_carlo.jl:128-137) on one colour class.
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (i >= count) return;
+    const int64_t d = start + i;
+    const int b = a.tb.pat[d];
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+    if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
+    const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+    const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
+    p.x[d] = -s.x + proj * H.x;
+    p.y[d] = -s.y + proj * H.y;
+    p.z[d] = -s.z + proj * H.z;
+}
+
+// deterministic_updates! body (monte_carlo.jl:205-210) on one colour class.
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (i >= count) return;
+    const int64_t d = start + i;
+    const int b = a.tb.pat[d];
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+    if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
+    const R n = Math<R>::sqrt_(H.x * H.x + H.y * H.y + H.z * H.z);
+    p.x[d] = -H.x / n * a.S;
+    p.y[d] = -H.y / n * a.S;
+    p.z[d] = -H.z / n * a.S;
+}
+
+// Per-block partial sums of total_energy (hamiltonian.jl:70-132).
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, double *part) {
+    __shared__ double scratch[GB / 32];
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    double e = 0.0;
+    if (d < a.tb.Np && a.dev2ref[d] >= 0) {
+        const int b = a.tb.pat[d];
+        e = site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+    }
+    e = block_sum<GB>(e, scratch);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = e;
+}
+
+// Per-block partial sums of sum_i s_i (observables.jl:12-18).
+template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArgs<R> a, int chain_lo, double *part) {
+    __shared__ double scratch[GB / 32];
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    double mx = 0, my = 0, mz = 0;
+    if (d < a.tb.Np) { // padding holds zero spins
+        mx = p.x[d];
+        my = p.y[d];
+        mz = p.z[d];
+    }
+    mx = block_sum<GB>(mx, scratch);
+    my = block_sum<GB>(my, scratch);
+    mz = block_sum<GB>(mz, scratch);
+    if (threadIdx.x == 0) {
+        int64_t o = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * 3;
+        part[o] = mx;
+        part[o + 1] = my;
+        part[o + 2] = mz;
+    }
+}
+
+// Deterministic fixed-order sum of per-block partials, one block per replica.
+// width = values per block entry (1: energy, 3: magnetisation -> norm).
+__global__ void k_reduce_rows(const double *part, int64_t nblk, int width, double *out_chain, int chain_base,
+                              int chain_lo) {
+    __shared__ double scratch[GB / 32];
+    const int row = blockIdx.x;
+    double v[3] = {0, 0, 0};
+    for (int64_t k = threadIdx.x; k < nblk; k += GB)
+        for (int q = 0; q < width; q++) v[q] += part[((int64_t)row * nblk + k) * width + q];
+    double t[3];
+    for (int q = 0; q < width; q++) t[q] = block_sum<GB>(v[q], scratch);
+    if (threadIdx.x == 0) {
+        double res = width == 1 ? t[0] : sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        out_chain[chain_base + chain_lo + row] = res;
+    }
+}
+
+// After one Metropolis sweep of replicas [chain_base+lo, +n): move the sweep's
+// accepted count into the slot counters and adapt sigma like
+// metropolis_adaptive! (metropolis.jl:124-126).
+__global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, double n_sites, double *last_acc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = chain_first + k;
+    const int slot = cs.slot_of[c];
+    const double a = (double)cs.sweep_acc[c];
+    cs.sweep_acc[c] = 0ull;
+    cs.acc_slot[slot] += a;
+    if (last_acc) last_acc[slot] = a;
+    if (kind == CSMC_METROPOLIS_ADAPTIVE) {
+        const double rate = a / n_sites;
+        const double om = 1 - rate;
+        const double f = 0.5 / (om > 0.05 ? om : 0.05);
+        double s = cs.sigma_slot[slot] * f;
+        s = s < 0.0 ? 0.0 : (s > 100 ? 100 : s);
+        cs.sigma_slot[slot] = s;
+    }
+}
+
+// Probe record: energy of the last Metropolis sweep and |M|, by slot.
+__global__ void k_probe_record(ChainState cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
+                               int n_slots) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int c = chain_first + q;
+    const int slot = cs.slot_of[c];
+    if (rec_E) rec_E[k * n_slots + slot] = cs.E_chain[c];
+    if (rec_M) rec_M[k * n_slots + slot] = cs.M_chain[c];
+}
+
+// Replica exchange of one lattice's slots (monte_carlo.jl:308-349): at
+// iteration `it` pairs (a, a+1) with a = (it/swap_rate) % 2 + 2m; the even
+// slot of the pair decides with probability min(1, exp(dbeta * dE)); an
+// accepted exchange swaps which replica sits in the two slots.
+__global__ void k_swap(ChainState cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
+                       uint32_t k0, uint32_t k1) {
+    const int phase = (int)((it / swap_rate) % 2);
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = phase + 2 * m, b = a + 1;
+    if (b >= n_rep) return;
+    const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
+    const int sa = slot_base + a, sb = slot_base + b;
+    const int se = slot_base + ev, so = slot_base + od;
+    const double Te = cs.T_slot[se], To = cs.T_slot[so];
+    const double Ee = cs.E_chain[cs.chain_of[se]], Eo = cs.E_chain[cs.chain_of[so]];
+    const double delta_beta = (1 / To - 1 / Te);
+    const double delta_E = (Eo - Ee);
+    const double x = exp(delta_beta * delta_E);
+    // counter (pair, iteration low word, lattice id ^ iteration high word, SWAP)
+    const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, sys_id ^ (uint32_t)(it >> 32), PURPOSE_SWAP, k0, k1);
+    if (u53(w.x, w.y) < (x < 1.0 ? x : 1.0)) {
+        const int ca = cs.chain_of[sa], cb = cs.chain_of[sb];
+        cs.chain_of[sa] = cb;
+        cs.chain_of[sb] = ca;
+        cs.slot_of[cb] = sa;
+        cs.slot_of[ca] = sb;
+        cs.exch_slot[sa] += 1;
+        cs.exch_slot[sb] += 1;
+    }
+}
+
+// Reference layout (interleaved FP64, reference order) <-> device order.
+template <typename R> __global__ void k_scatter(SysArgs<R> a, int chain_lo, const double *src) {
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np) return;
+    const int64_t i = a.dev2ref[d];
+    if (i < 0) return;
+    const double *s = src + ((int64_t)blockIdx.y * a.n_real + i) * 3;
+    p.x[d] = (R)s[0];
+    p.y[d] = (R)s[1];
+    p.z[d] = (R)s[2];
+}
+
+template <typename R> __global__ void k_gather(SysArgs<R> a, int chain_lo, double *dst) {
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np) return;
+    const int64_t i = a.dev2ref[d];
+    if (i < 0) return;
+    double *s = dst + ((int64_t)blockIdx.y * a.n_real + i) * 3;
+    s[0] = (double)p.x[d];
+    s[1] = (double)p.y[d];
+    s[2] = (double)p.z[d];
+}
+
+// Uniform spins from the INIT stream, counter (reference site, 0, chain, INIT).
+template <typename R> __global__ void k_random_spins(SysArgs<R> a, uint32_t k0, uint32_t k1) {
+    const int r = blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np) return;
+    const int64_t i = a.dev2ref[d];
+    if (i < 0) return;
+    const U4 w = philox4x32_10((uint32_t)i, 0u, (uint32_t)(a.chain_base + r), PURPOSE_INIT, k0, k1);
+    const double uphi = u53(w.x, w.y), uz = u53(w.z, w.w);
+    double sp, cp;
+    sincospi(2.0 * uphi, &sp, &cp);
+    const double z = 2.0 * uz - 1.0;
+    const double rr = sqrt(fmax(1.0 - z * z, 0.0));
+    const double S = (double)a.S;
+    p.x[d] = (R)(S * (rr * cp));
+    p.y[d] = (R)(S * (rr * sp));
+    p.z[d] = (R)(S * z);
+}
+
+template <typename R, bool CUB, bool QUA> __global__ void k_local_field(SysArgs<R> a, int r, double *out) {
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np) return;
+    const int64_t i = a.dev2ref[d];
+    if (i < 0) return;
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, a.tb.pat[d]);
+    out[3 * i] = (double)H.x;
+    out[3 * i + 1] = (double)H.y;
+    out[3 * i + 2] = (double)H.z;
+}
+
+template <typename R, bool CUB, bool QUA>
+__global__ void k_energy_diff(SysArgs<R> a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE) {
+    const Ptrs<R> p = replica(a, r);
+    const int64_t q = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (q >= n) return;
+    const int64_t d = a.ref2dev[sites[q]];
+    const int b = a.tb.pat[d];
+    V3<R> hb, hc, hq;
+    partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b, hb, hc, hq);
+    const R *h = a.cf.h + 3 * b;
+    const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+    const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+    const V3<R> sn = {(R)ns[3 * q], (R)ns[3 * q + 1], (R)ns[3 * q + 2]};
+    dE[q] = (double)delta_e<R>(a.cf, b, s, sn, hext);
+}
+
+template <typename R> __global__ void k_renorm(SysArgs<R> a, int chain_lo) {
+    const int r = chain_lo + blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np || a.dev2ref[d] < 0) return;
+    const R x = p.x[d], y = p.y[d], z = p.z[d];
+    const R n2 = x * x + y * y + z * z;
+    if (n2 == R(0)) return;
+    const R f = a.S * Math<R>::rsqrt_(n2);
+    p.x[d] = x * f;
+    p.y[d] = y * f;
+    p.z[d] = z * f;
+}
+
+template <typename R> __global__ void k_drift(SysArgs<R> a, unsigned int *bits) {
+    const int r = blockIdx.y;
+    const Ptrs<R> p = replica(a, r);
+    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (d >= a.tb.Np || a.dev2ref[d] < 0) return;
+    const double x = p.x[d], y = p.y[d], z = p.z[d];
+    const double S = (double)a.S;
+    const float e = (float)(fabs(sqrt(x * x + y * y + z * z) - S) / (S != 0 ? S : 1.0));
+    atomicMax(bits, __float_as_uint(e));
+}
+
+// ------------------------------------------------------------ resident path
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// Bulk TMA copy global -> shared, completion counted on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase: gives up after `limit` polls and
+// reports it through the context's error flag instead of hanging.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *error_flag) {
+    for (int k = 0; k < (1 << 22); k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (threadIdx.x == 0) atomicExch(error_flag, 1);
+    return false;
+}
+
+template <typename R, bool CUB, bool QUA, int NT> struct Resident {
+    const ResSys<R> &S;
+    R *x, *y, *z;
+    double *scratch;
+    int c, slot;
+
+    __device__ __forceinline__ void barrier() const { __syncthreads(); }
+
+    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
+        unsigned acc = 0;
+        for (int col = 0; col < S.n_colours; col++) {
+            const int64_t st = S.col_start[col], n = S.col_count[col];
+            for (int64_t i = threadIdx.x; i < n; i += NT) {
+                const int64_t d = st + i;
+                const int b = S.tb.pat[d];
+                V3<R> hb, hc, hq;
+                partner_fields<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, b, hb, hc, hq);
+                const R *h = S.cf.h + 3 * b;
+                const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+                const V3<R> s = {x[d], y[d], z[d]};
+                const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1);
+                const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
+                const R dE = delta_e<R>(S.cf, b, s, sn, hext);
+                bool accept = dE < R(0);
+                if (!accept) {
+                    const R arg = sizeof(R) == 4 ? -dE * invT : -dE / (R)T;
+                    accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
+                }
+                if (accept) {
+                    x[d] = sn.x;
+                    y[d] = sn.y;
+                    z[d] = sn.z;
+                    acc++;
+                }
+            }
+            barrier();
+        }
+        return acc;
+    }
+
+    __device__ void or_sweep() const {
+        for (int col = 0; col < S.n_colours; col++) {
+            const int64_t st = S.col_start[col], n = S.col_count[col];
+            for (int64_t i = threadIdx.x; i < n; i += NT) {
+                const int64_t d = st + i;
+                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
+                if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
+                const V3<R> s = {x[d], y[d], z[d]};
+                const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
+                x[d] = -s.x + proj * H.x;
+                y[d] = -s.y + proj * H.y;
+                z[d] = -s.z + proj * H.z;
+            }
+            barrier();
+        }
+    }
+
+    __device__ double energy() const { // valid in thread 0
+        double e = 0.0;
+        for (int col = 0; col < S.n_colours; col++) {
+            const int64_t st = S.col_start[col], n = S.col_count[col];
+            for (int64_t i = threadIdx.x; i < n; i += NT) {
+                const int64_t d = st + i;
+                e += site_energy_share<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
+            }
+        }
+        return block_sum<NT>(e, scratch);
+    }
+
+    __device__ double magnetization() const { // valid in thread 0
+        double mx = 0, my = 0, mz = 0;
+        const int64_t Np = S.tb.Np;
+        for (int64_t d = threadIdx.x; d < Np; d += NT) { // padding holds zeros
+            mx += x[d];
+            my += y[d];
+            mz += z[d];
+        }
+        mx = block_sum<NT>(mx, scratch);
+        my = block_sum<NT>(my, scratch);
+        mz = block_sum<NT>(mz, scratch);
+        return sqrt(mx * mx + my * my + mz * mz);
+    }
+
+    __device__ void renormalize() const {
+        for (int col = 0; col < S.n_colours; col++) {
+            const int64_t st = S.col_start[col], n = S.col_count[col];
+            for (int64_t i = threadIdx.x; i < n; i += NT) {
+                const int64_t d = st + i;
+                const R a = x[d], b = y[d], cc = z[d];
+                const R n2 = a * a + b * b + cc * cc;
+                if (n2 == R(0)) continue;
+                const R f = S.S * Math<R>::rsqrt_(n2);
+                x[d] = a * f;
+                y[d] = b * f;
+                z[d] = cc * f;
+            }
+        }
+        barrier();
+    }
+};
+
+// Probe of iteration q exists?  (q >= t_therm and q % probe_rate == 0)
+__device__ __forceinline__ bool is_probe(const RunDesc &rd, int64_t q) {
+    return rd.probe_rate > 0 && q >= rd.t_therm && q % rd.probe_rate == 0;
+}
+
+template <typename R, bool CUB, bool QUA, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    k_resident(const ResSys<R> *__restrict__ systems, const int2 *__restrict__ items, int n_items, int *work_ctr,
+               ChainState cs, RunDesc rd) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bar;
+    __shared__ double scratch[32];
+    __shared__ int s_item;
+    __shared__ double s_sigma;
+    __shared__ ResSys<R> s_sys;
+    uint32_t parity = 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int64_t dosweep = rd.or_rate == 0 ? 1 : rd.or_rate;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(work_ctr, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items) break;
+        const int2 w = items[item];
+        if (threadIdx.x == 0) s_sys = systems[w.x];
+        __syncthreads();
+        const ResSys<R> &S = s_sys;
+        const int r = w.y;
+        const int c = S.chain_base + r;
+        const int64_t Np = S.tb.Np;
+        R *gx = S.spins + (int64_t)r * 3 * Np;
+        R *x = reinterpret_cast<R *>(smem_raw), *y = x + Np, *z = y + Np;
+
+        // stage the replica: three bulk TMA copies of Np elements
+        if (threadIdx.x == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const uint32_t bytes = (uint32_t)(Np * sizeof(R));
+            mbar_expect_tx(&bar, 3 * bytes);
+            bulk_g2s(x, gx, bytes, &bar);
+            bulk_g2s(y, gx + Np, bytes, &bar);
+            bulk_g2s(z, gx + 2 * Np, bytes, &bar);
+        }
+        const bool ok = mbar_wait_bounded(&bar, parity, cs.error_flag);
+        parity ^= 1;
+        if (__syncthreads_or(!ok)) { // block-uniform: wait once more for the copies in flight, drop the item
+            mbar_wait_bounded(&bar, parity ^ 1, cs.error_flag);
+            __syncthreads();
+            continue;
+        }
+
+        const int slot = cs.slot_of[c];
+        const double T = rd.T_override > 0 ? rd.T_override : cs.T_slot[slot];
+        if (threadIdx.x == 0) s_sigma = rd.reset_sigma ? rd.sigma0 : cs.sigma_slot[slot];
+        __syncthreads();
+        Resident<R, CUB, QUA, NT> k{S, x, y, z, scratch, c, slot};
+        const R invT = (R)(1.0 / T);
+        double E = cs.E_chain[c];
+        double acc_total = 0.0;
+        uint32_t msweep = rd.msweep0;
+        int sweeps_since_renorm = 0;
+
+        if (rd.pending_probe) { // probe of the exchange iteration it0-1
+            const int64_t q = rd.it0 - 1;
+            const double M = k.magnetization();
+            if (threadIdx.x == 0) {
+                const int64_t kq = (q - rd.probe_first) / rd.probe_rate;
+                if (kq >= 0 && kq < rd.probe_cap) {
+                    if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
+                    if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
+                }
+                cs.M_chain[c] = M;
+            }
+        }
+
+        for (int64_t it = rd.it0; it < rd.it1; it++) {
+            if (rd.or_rate != 0) {
+                k.or_sweep();
+                sweeps_since_renorm++;
+            }
+            const bool metro = it % dosweep == 0;
+            if (metro) {
+                const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
+                msweep++;
+                sweeps_since_renorm++;
+                const double at = block_sum<NT>((double)a, scratch);
+                if (threadIdx.x == 0) {
+                    acc_total += at;
+                    if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) {
+                        const double om = 1 - at / (double)S.n_real;
+                        const double f = 0.5 / (om > 0.05 ? om : 0.05);
+                        double sg = s_sigma * f;
+                        s_sigma = sg < 0.0 ? 0.0 : (sg > 100 ? 100 : sg);
+                    }
+                }
+                __syncthreads();
+                // energy needed: exchange point, a probe before the next
+                // Metropolis sweep, or the last Metropolis sweep of the window
+                bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
+                for (int64_t q = it; q < it + dosweep && q < rd.it1 && !needE; q++) needE = is_probe(rd, q);
+                needE = needE || it + dosweep >= rd.it1;
+                if (needE) {
+                    const double e = k.energy();
+                    if (threadIdx.x == 0) E = e;
+                }
+            }
+            const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
+            if (is_probe(rd, it) && !swap_here) {
+                const double M = k.magnetization();
+                if (threadIdx.x == 0) {
+                    const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
+                    if (kq >= 0 && kq < rd.probe_cap) {
+                        if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
+                        if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
+                    }
+                    cs.M_chain[c] = M;
+                }
+            }
+            if (sizeof(R) == 4 && rd.renorm_every > 0 && sweeps_since_renorm >= rd.renorm_every) {
+                k.renormalize();
+                sweeps_since_renorm = 0;
+            }
+        }
+        if (sizeof(R) == 4 && rd.renorm_every > 0 && sweeps_since_renorm > 0) k.renormalize();
+
+        if (threadIdx.x == 0) {
+            cs.E_chain[c] = E;
+            cs.acc_slot[slot] += acc_total;
+            cs.sigma_slot[slot] = s_sigma;
+        }
+        __syncthreads();
+        // write the replica back (x, y, z are contiguous in both memories)
+        for (int64_t i = threadIdx.x; i < 3 * Np; i += NT) gx[i] = x[i];
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+template <typename R> static dim3 grid_for(int64_t n, int chains) {
+    return dim3((unsigned)((n + GB - 1) / GB), (unsigned)chains);
+}
+
+#define DISPATCH_CQ(a, KERNEL, ...)                                                                                    \
+    do {                                                                                                               \
+        if ((a).cub && (a).qua) KERNEL<R, true, true> __VA_ARGS__;                                                     \
+        else if ((a).cub) KERNEL<R, true, false> __VA_ARGS__;                                                          \
+        else if ((a).qua) KERNEL<R, false, true> __VA_ARGS__;                                                          \
+        else KERNEL<R, false, false> __VA_ARGS__;                                                                      \
+    } while (0)
+
+template <typename R>
+void launch_metro_colour(const SysArgs<R> &a, const ChainState &cs, int64_t start, int64_t count, int chain_lo,
+                         int n_chains, int kind, uint32_t msweep, double T_override, cudaStream_t st) {
+    if (count <= 0 || n_chains <= 0) return;
+    dim3 g = grid_for<R>(count, n_chains);
+    DISPATCH_CQ(a, k_metro_colour, <<<g, GB, 0, st>>>(a, cs, start, count, chain_lo, kind, msweep, T_override));
+}
+
+template <typename R>
+void launch_or_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
+                      cudaStream_t st) {
+    if (count <= 0 || n_chains <= 0) return;
+    dim3 g = grid_for<R>(count, n_chains);
+    DISPATCH_CQ(a, k_or_colour, <<<g, GB, 0, st>>>(a, start, count, chain_lo));
+}
+
+template <typename R>
+void launch_det_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
+                       cudaStream_t st) {
+    if (count <= 0 || n_chains <= 0) return;
+    dim3 g = grid_for<R>(count, n_chains);
+    DISPATCH_CQ(a, k_det_colour, <<<g, GB, 0, st>>>(a, start, count, chain_lo));
+}
+
+int64_t partial_blocks(int64_t Np) { return (Np + GB - 1) / GB; }
+
+template <typename R>
+void launch_energy(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
+                   cudaStream_t st) {
+    if (n_chains <= 0) return;
+    dim3 g = grid_for<R>(a.tb.Np, n_chains);
+    DISPATCH_CQ(a, k_energy_part, <<<g, GB, 0, st>>>(a, chain_lo, part));
+    k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 1, cs.E_chain, a.chain_base, chain_lo);
+}
+
+template <typename R>
+void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
+                   cudaStream_t st) {
+    if (n_chains <= 0) return;
+    dim3 g = grid_for<R>(a.tb.Np, n_chains);
+    k_magnet_part<R><<<g, GB, 0, st>>>(a, chain_lo, part);
+    k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 3, cs.M_chain, a.chain_base, chain_lo);
+}
+
+void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double *last_acc,
+                        cudaStream_t st) {
+    if (n <= 0) return;
+    k_after_metro<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, kind, (double)n_sites, last_acc);
+}
+
+void launch_probe_record(const ChainState &cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
+                         int n_slots, cudaStream_t st) {
+    if (n <= 0) return;
+    k_probe_record<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, rec_E, rec_M, k, n_slots);
+}
+
+void launch_swap(const ChainState &cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
+                 uint32_t k0, uint32_t k1, cudaStream_t st) {
+    const int pairs = n_rep / 2 + 1;
+    k_swap<<<(pairs + 127) / 128, 128, 0, st>>>(cs, slot_base, n_rep, it, swap_rate, sys_id, k0, k1);
+}
+
+template <typename R> void launch_scatter(const SysArgs<R> &a, int chain_lo, int n_chains, const double *src, cudaStream_t st) {
+    k_scatter<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo, src);
+}
+template <typename R> void launch_gather(const SysArgs<R> &a, int chain_lo, int n_chains, double *dst, cudaStream_t st) {
+    k_gather<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo, dst);
+}
+template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st) {
+    k_random_spins<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, k0, k1);
+}
+template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st) {
+    dim3 g = grid_for<R>(a.tb.Np, 1);
+    DISPATCH_CQ(a, k_local_field, <<<g, GB, 0, st>>>(a, r, out));
+}
+template <typename R>
+void launch_energy_diff(const SysArgs<R> &a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE,
+                        cudaStream_t st) {
+    if (n <= 0) return;
+    dim3 g = grid_for<R>(n, 1);
+    DISPATCH_CQ(a, k_energy_diff, <<<g, GB, 0, st>>>(a, r, n, sites, ns, dE));
+}
+template <typename R> void launch_renorm(const SysArgs<R> &a, int chain_lo, int n_chains, cudaStream_t st) {
+    k_renorm<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo);
+}
+template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits, cudaStream_t st) {
+    k_drift<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, bits);
+}
+
+template <typename R, int NT> static const void *resident_fn(bool cub, bool qua) {
+    if (cub && qua) return (const void *)k_resident<R, true, true, NT>;
+    if (cub) return (const void *)k_resident<R, true, false, NT>;
+    if (qua) return (const void *)k_resident<R, false, true, NT>;
+    return (const void *)k_resident<R, false, false, NT>;
+}
+
+template <typename R>
+cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
+                            const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem, bool cub,
+                            bool qua, cudaStream_t st) {
+    const void *fn = block == 1024 ? resident_fn<R, 1024>(cub, qua)
+                     : block == 256 ? resident_fn<R, 256>(cub, qua)
+                                    : resident_fn<R, 512>(cub, qua);
+    // work_ctr must be zero when the kernel starts (the caller resets it on `st`)
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ChainState csv = cs;
+    RunDesc rdv = rd;
+    void *args[] = {(void *)&d_sys, (void *)&items, (void *)&n_items, (void *)&work_ctr, (void *)&csv, (void *)&rdv};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st);
+}
+
+template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, bool cub, bool qua) {
+    const void *fn = block == 1024 ? resident_fn<R, 1024>(cub, qua)
+                     : block == 256 ? resident_fn<R, 256>(cub, qua)
+                                    : resident_fn<R, 512>(cub, qua);
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+#define INSTANTIATE(R)                                                                                                 \
+    template void launch_metro_colour<R>(const SysArgs<R> &, const ChainState &, int64_t, int64_t, int, int, int,     \
+                                         uint32_t, double, cudaStream_t);                                              \
+    template void launch_or_colour<R>(const SysArgs<R> &, int64_t, int64_t, int, int, cudaStream_t);                  \
+    template void launch_det_colour<R>(const SysArgs<R> &, int64_t, int64_t, int, int, cudaStream_t);                 \
+    template void launch_energy<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \
+    template void launch_magnet<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \
+    template void launch_scatter<R>(const SysArgs<R> &, int, int, const double *, cudaStream_t);                      \
+    template void launch_gather<R>(const SysArgs<R> &, int, int, double *, cudaStream_t);                             \
+    template void launch_random_spins<R>(const SysArgs<R> &, uint32_t, uint32_t, cudaStream_t);                       \
+    template void launch_local_field<R>(const SysArgs<R> &, int, double *, cudaStream_t);                             \
+    template void launch_energy_diff<R>(const SysArgs<R> &, int, int64_t, const int64_t *, const double *, double *,  \
+                                        cudaStream_t);                                                                 \
+    template void launch_renorm<R>(const SysArgs<R> &, int, int, cudaStream_t);                                       \
+    template void launch_drift<R>(const SysArgs<R> &, unsigned int *, cudaStream_t);                                  \
+    template cudaError_t launch_resident<R>(const ResSys<R> *, const int2 *, int, int *, const ChainState &,          \
+                                            const RunDesc &, int, int, size_t, bool, bool, cudaStream_t);             \
+    template int resident_max_blocks_per_sm<R>(int, size_t, bool, bool);
+
+INSTANTIATE(float)
+INSTANTIATE(double)
+
+} // namespace csmc

@@ -1,0 +1,71 @@
+// kernels.cuh -- launch-side declarations of the sweep kernels (kernels.cu)
+// and the replay kernel (exact.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace csmc {
+
+// Per-replica state, context-wide device arrays.  Slots are temperature
+// slots (MPI ranks of the reference); chains are physical replicas.
+struct ChainState {
+    int32_t *slot_of;  // chain -> slot
+    int32_t *chain_of; // slot -> chain
+    double *T_slot, *sigma_slot;
+    double *acc_slot, *exch_slot;
+    double *E_chain, *M_chain;
+    unsigned long long *sweep_acc; // accepted proposals of the current sweep, per chain
+    unsigned int *drift_bits;      // max relative |S| error, float bits
+    int *error_flag;               // nonzero: a bounded wait gave up
+};
+
+// One lattice for the global-memory kernels.
+template <typename R> struct SysArgs {
+    Tab<uint32_t> tb;
+    Coef<R> cf;
+    R *spins; // replica r at spins + r * 3 * Np (x, y, z blocks of Np)
+    const int32_t *dev2ref;
+    const int64_t *ref2dev;
+    int32_t chain_base, n_rep;
+    int64_t n_real; // real sites
+    R S;
+    uint32_t k0, k1; // Philox key (seed)
+    int cub, qua;
+};
+
+// One lattice for the resident kernel (lives in device memory).
+template <typename R> struct ResSys {
+    Tab<uint16_t> tb;
+    Coef<R> cf;
+    R *spins;
+    int32_t chain_base, n_rep;
+    int32_t n_colours, nb;
+    int64_t col_start[CSMC_MAX_COLOURS + 1];
+    int64_t col_count[CSMC_MAX_COLOURS];
+    int64_t n_real;
+    R S;
+    uint32_t k0, k1;
+};
+
+// The sweep schedule of one resident launch (see csmc_run_params).
+struct RunDesc {
+    int64_t it0, it1;         // iterations [it0, it1)
+    int64_t t_therm;
+    int64_t probe_first;      // iteration of probe record 0
+    int64_t probe_cap;
+    double *rec_E, *rec_M;    // [probe_cap][n_slots]
+    double T_override;        // > 0: this temperature for every replica (annealing)
+    double sigma0;
+    uint32_t msweep0;         // Metropolis sweep counter at the first Metropolis sweep
+    int32_t or_rate, swap_rate, probe_rate, kind;
+    int32_t pending_probe;    // record the probe of iteration it0-1 first
+    int32_t reset_sigma;      // sigma <- sigma0 before the first sweep
+    int32_t n_slots;
+    int32_t renorm_every;     // single precision: renormalise every k sweeps
+    int32_t swap_enabled;
+};
+
+} // namespace csmc

@@ -1,0 +1,65 @@
+// launch.hpp -- host launchers of the kernels in kernels.cu and exact.cu.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace csmc {
+
+template <typename R>
+void launch_metro_colour(const SysArgs<R> &a, const ChainState &cs, int64_t start, int64_t count, int chain_lo,
+                         int n_chains, int kind, uint32_t msweep, double T_override, cudaStream_t st);
+template <typename R>
+void launch_or_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
+                      cudaStream_t st);
+template <typename R>
+void launch_det_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
+                       cudaStream_t st);
+int64_t partial_blocks(int64_t Np);
+// total_energy of replicas [chain_lo, chain_lo+n) into cs.E_chain; part needs
+// n * partial_blocks(Np) doubles
+template <typename R>
+void launch_energy(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
+                   cudaStream_t st);
+// |M| into cs.M_chain; part needs 3 * n * partial_blocks(Np) doubles
+template <typename R>
+void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
+                   cudaStream_t st);
+void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double *last_acc,
+                        cudaStream_t st);
+void launch_probe_record(const ChainState &cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
+                         int n_slots, cudaStream_t st);
+void launch_swap(const ChainState &cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
+                 uint32_t k0, uint32_t k1, cudaStream_t st);
+template <typename R>
+void launch_scatter(const SysArgs<R> &a, int chain_lo, int n_chains, const double *src, cudaStream_t st);
+template <typename R> void launch_gather(const SysArgs<R> &a, int chain_lo, int n_chains, double *dst, cudaStream_t st);
+template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st);
+template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st);
+template <typename R>
+void launch_energy_diff(const SysArgs<R> &a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE,
+                        cudaStream_t st);
+template <typename R> void launch_renorm(const SysArgs<R> &a, int chain_lo, int n_chains, cudaStream_t st);
+template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits, cudaStream_t st);
+template <typename R>
+cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
+                            const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem, bool cub,
+                            bool qua, cudaStream_t st);
+template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, bool cub, bool qua);
+
+// Reference-layout tables of one lattice for the replay kernel (exact.cu):
+// per reference site, N2/N3/N4 term entries with 0-based partners (-1 absent).
+struct ExactTables {
+    int64_t N;
+    int N2, N3, N4;
+    const int64_t *bs, *cs, *qs;
+    const double *bm, *ct, *qt, *field, *onsite;
+    const int64_t *ref2dev;
+    int64_t Np;
+    double S;
+};
+// Sequential FP64 replay of n proposals on the FP64 replica at `spins`.
+void launch_replay(const ExactTables &t, double *spins, int kind, double T, double *sigma_dev, int64_t n,
+                   const int64_t *sites, const double *u_phi, const double *u_z, const double *u_acc,
+                   uint8_t *accepted, cudaStream_t st);
+
+} // namespace csmc

@@ -1,0 +1,436 @@
+"""MonteCarlo and the sweep drivers, mirroring metropolis.jl, monte_carlo.jl,
+hamiltonian.jl and observables.jl on top of the GPU library.
+
+``MonteCarlo(T, lattice, parameters)`` creates a device context holding the
+lattice's flattened tables and one replica per temperature: ``T`` may be a
+single temperature (the reference's one MPI rank) or a sequence (the ranks of
+a parallel-tempering ladder, batched on the one GPU).  Spins live on the
+device; ``mc.lattice.spins`` is refreshed after every driver call.
+
+The sweep plug point of the reference, ``alg(mc, T)``
+(``alg::FunctionWrapper{Float64,Tuple{MonteCarlo,Float64}}``, metropolis.jl:181-199),
+is kept: ``Metropolis()``, ``MetropolisAdaptive()`` and
+``MetropolisFixedCone()`` return callables that run one device sweep and
+return the accepted count.  The constrained variants call an arbitrary host
+closure per proposal (metropolis.jl:36-58, :155-179) and are not provided.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import math
+import warnings
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .lattice import Lattice
+from .observables import Observables, mean_and_error, specific_heat, susceptibility
+
+
+@dataclass
+class SimulationParameters:
+    """SimulationParameters (metropolis.jl:4-13)."""
+
+    t_thermalization: int = 1
+    t_deterministic: int = 1
+    t_measurement: int = 1
+    probe_rate: int = 1
+    swap_rate: int = 1
+    overrelaxation_rate: int = 10
+    report_interval: int = 0
+    checkpoint_rate: int = 0
+
+
+_ALLOWED = ["t_thermalization", "t_deterministic", "t_measurement", "probe_rate", "swap_rate",
+            "overrelaxation_rate", "report_interval", "checkpoint_rate"]
+
+
+def MCParamsBuffer(d: dict) -> SimulationParameters:
+    """MCParamsBuffer (monte_carlo.jl:10-27): defaults, and a warning per unknown key."""
+    for key in d:
+        if key not in _ALLOWED:
+            warnings.warn(f"'{key}' not a valid MC parameter; ignoring")
+    return SimulationParameters(**{k: int(d[k]) for k in _ALLOWED if k in d})
+
+
+class _Alg:
+    """A Metropolis sweep kind usable as alg(mc, T)."""
+
+    def __init__(self, kind: int, name: str):
+        self.kind = kind
+        self.name = name
+
+    def __call__(self, mc: "MonteCarlo", T=None):
+        return mc._metropolis(self.kind, T)
+
+    def __repr__(self):
+        return f"{self.name}()"
+
+
+def Metropolis() -> _Alg:
+    """Metropolis() -> metropolis! (metropolis.jl:65-82, :181-183)."""
+    return _Alg(_lib.METROPOLIS, "Metropolis")
+
+
+def MetropolisAdaptive() -> _Alg:
+    """MetropolisAdaptive() -> metropolis_adaptive! (metropolis.jl:113-133, :185-187)."""
+    return _Alg(_lib.METROPOLIS_ADAPTIVE, "MetropolisAdaptive")
+
+
+def MetropolisFixedCone() -> _Alg:
+    """MetropolisFixedCone() -> metropolis_fixed_cone! (metropolis.jl:136-153, :189-191)."""
+    return _Alg(_lib.METROPOLIS_FIXED_CONE, "MetropolisFixedCone")
+
+
+_PRECISION = {"fp64": _lib.FP64, "fp32": _lib.FP32}
+_PATHS = {"auto": _lib.PATH_AUTO, "resident": _lib.PATH_RESIDENT, "global": _lib.PATH_GLOBAL,
+          "per_replica": _lib.PATH_PER_REPLICA}
+
+
+class Context:
+    """Owner of one libcsmc context (csmc_create / csmc_destroy)."""
+
+    def __init__(self, lattices, replicas, precision="fp64", seed=20261203):
+        lattices = list(lattices)
+        self.lattices = lattices
+        self.replicas = [int(r) for r in replicas]
+        self.precision = precision
+        self.handle = C.c_void_p()
+        descs = (_lib.LatticeDesc * len(lattices))(*[l.desc.desc for l in lattices])
+        reps = np.asarray(self.replicas, dtype=np.int32)
+        _lib.call("csmc_create_batch", descs, len(lattices), _lib.ptr(reps, C.c_int32), _PRECISION[precision],
+                  C.c_uint64(seed), C.byref(self.handle))
+        n = C.c_int32()
+        _lib.call("csmc_num_slots", self.handle, C.byref(n))
+        self.n_slots = n.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().csmc_destroy(h)
+            except Exception:
+                pass
+            self.handle = C.c_void_p()
+
+    def call(self, name, *args):
+        _lib.call(name, self.handle, *args)
+
+    def slot_sizes(self):
+        out = []
+        for l, r in zip(self.lattices, self.replicas):
+            out += [l.size] * r
+        return out
+
+    def set_spins(self, slot: int, spins: np.ndarray):
+        s = np.asfortranarray(spins, dtype=np.float64)
+        self.call("csmc_set_spins", int(slot), _lib.ptr(s, C.c_double))
+
+    def get_spins(self, slot: int) -> np.ndarray:
+        n = self.slot_sizes()[slot]
+        s = np.zeros((3, n), np.float64, order="F")
+        self.call("csmc_get_spins", int(slot), _lib.ptr(s, C.c_double))
+        return s
+
+    def set_temperatures(self, T):
+        t = np.ascontiguousarray(T, dtype=np.float64)
+        self.call("csmc_set_temperatures", _lib.ptr(t, C.c_double))
+
+    def per_slot(self, name) -> np.ndarray:
+        out = np.zeros(self.n_slots, np.float64)
+        self.call(name, _lib.ptr(out, C.c_double))
+        return out
+
+
+class MonteCarlo:
+    """MonteCarlo(T, lattice, parameters; ...) (monte_carlo.jl:56-118).
+
+    Extra keywords of this implementation: ``precision`` ("fp64" or "fp32"),
+    ``seed`` (Philox key), ``path`` ("auto", "resident", "global",
+    "per_replica").  Output files (``outpath``) are not written by this
+    package; pass ``outpath=""`` (the default).
+    """
+
+    def __init__(self, T, lattice: Lattice, parameters: dict, *, constraint=None, weight: float = 0.0,
+                 outpath: str = "", outprefix: str = "configuration", inparams=None, overwrite: bool = True,
+                 sigma0: float = 60, corr: bool = False, ks=None, precision: str = "fp64", seed: int = 20261203,
+                 path: str = "auto"):
+        if corr and (ks is None or np.asarray(ks).shape[1] == 0):
+            raise ValueError("No momentum vectors provided for correlation calculations!")
+        if constraint is not None and weight != 0.0:
+            raise NotImplementedError("constrained Metropolis (metropolis.jl:36-58) is not provided")
+        if outpath:
+            warnings.warn("outpath given: HDF5 output is not written by this package")
+        self.temperatures = np.atleast_1d(np.asarray(T, dtype=np.float64)).copy()
+        self.lattice = copy.deepcopy(lattice)  # monte_carlo.jl:74
+        self.parameters = MCParamsBuffer(dict(parameters))
+        self.sigma0 = float(sigma0)
+        self.outpath = outpath
+        self.path = path
+        R = len(self.temperatures)
+        self.ctx = Context([self.lattice], [R], precision=precision, seed=seed)
+        self.ctx.set_temperatures(self.temperatures)
+        self.ctx.call("csmc_set_sigma", _lib.ptr(np.full(R, self.sigma0), C.c_double))
+        for r in range(R):
+            self.ctx.set_spins(r, self.lattice.spins)
+        self.observables = [Observables() for _ in range(R)]
+        self.accepted = np.zeros(R)
+        self.exchanged = np.zeros(R)
+
+    # -- state --------------------------------------------------------------
+    @property
+    def T(self):
+        return float(self.temperatures[0]) if len(self.temperatures) == 1 else self.temperatures
+
+    @property
+    def n_replicas(self) -> int:
+        return len(self.temperatures)
+
+    @property
+    def sigma(self):
+        s = self.ctx.per_slot("csmc_get_sigma")
+        return float(s[0]) if len(s) == 1 else s
+
+    def spins(self, slot: int = 0) -> np.ndarray:
+        return self.ctx.get_spins(slot)
+
+    def set_spins(self, spins: np.ndarray, slot: int = 0) -> None:
+        self.ctx.set_spins(slot, spins)
+        if slot == 0:
+            self.lattice.spins[:] = spins
+
+    def sync(self) -> None:
+        self.lattice.spins = self.ctx.get_spins(0)
+
+    # -- plug point ---------------------------------------------------------
+    def _metropolis(self, kind: int, T=None):
+        if T is not None and self.n_replicas == 1 and float(T) != self.temperatures[0]:
+            self.temperatures[0] = float(T)
+            self.ctx.set_temperatures(self.temperatures)
+        acc = np.zeros(self.n_replicas)
+        self.ctx.call("csmc_metropolis_sweep", int(kind), _lib.ptr(acc, C.c_double))
+        self.sync()
+        return float(acc[0]) if self.n_replicas == 1 else acc
+
+
+def _context_of(x):
+    """A MonteCarlo's context, or a cached FP64 context for a bare Lattice with its spins uploaded."""
+    if isinstance(x, MonteCarlo):
+        return x.ctx, x
+    lat = x
+    ctx = getattr(lat, "_ctx", None)
+    if ctx is None:
+        ctx = Context([lat], [1], precision="fp64")
+        lat._ctx = ctx
+    ctx.set_spins(0, lat.spins)
+    return ctx, None
+
+
+def overrelaxation(x) -> None:
+    """overrelaxation! (monte_carlo.jl:126-139): one sweep, colour class by colour class."""
+    ctx, mc = _context_of(x)
+    ctx.call("csmc_overrelax_sweep")
+    if mc is None:
+        x.spins[:] = ctx.get_spins(0)
+    else:
+        mc.sync()
+
+
+def total_energy(x, slot: int = 0) -> float:
+    """total_energy (hamiltonian.jl:70-132)."""
+    ctx, _ = _context_of(x)
+    return float(ctx.per_slot("csmc_total_energy")[slot])
+
+
+def energy_density(x, slot: int = 0) -> float:
+    """energy_density (hamiltonian.jl:134-136)."""
+    ctx, mc = _context_of(x)
+    n = (mc.lattice if mc else x).size
+    return float(ctx.per_slot("csmc_total_energy")[slot]) / n
+
+
+def get_magnetization(x, slot: int = 0) -> float:
+    """get_magnetization (observables.jl:12-18): |sum_i s_i|."""
+    ctx, _ = _context_of(x)
+    return float(ctx.per_slot("csmc_magnetization")[slot])
+
+
+def get_local_field(x, point: int, slot: int = 0) -> tuple:
+    """get_local_field (hamiltonian.jl:3-67) at 1-based site `point`."""
+    ctx, mc = _context_of(x)
+    n = (mc.lattice if mc else x).size
+    H = np.zeros((3, n), np.float64, order="F")
+    ctx.call("csmc_local_field", int(slot), _lib.ptr(H, C.c_double))
+    return tuple(float(v) for v in H[:, point - 1])
+
+
+def local_fields(x, slot: int = 0) -> np.ndarray:
+    """get_local_field at every site, as a 3 x N array."""
+    ctx, mc = _context_of(x)
+    n = (mc.lattice if mc else x).size
+    H = np.zeros((3, n), np.float64, order="F")
+    ctx.call("csmc_local_field", int(slot), _lib.ptr(H, C.c_double))
+    return H
+
+
+def annealing_temperatures(schedule, T0: float, T_target: float) -> list[float]:
+    """The temperatures simulated_annealing! visits: T0, schedule(1), ... while T > target (monte_carlo.jl:159-185)."""
+    temps, T, time = [], T0, 1
+    while T > T_target:
+        temps.append(T)
+        T = schedule(time)
+        time += 1
+    return temps
+
+
+def simulated_annealing(mc: MonteCarlo, schedule, T0: float = 1.0, alg: _Alg | None = None,
+                        verbose: bool = True) -> np.ndarray:
+    """simulated_annealing! (monte_carlo.jl:157-190).
+
+    Every replica anneals through the same temperature sequence down to the
+    MonteCarlo's target temperature (all replicas must share it).  Returns the
+    accepted proposals per temperature and replica.
+    """
+    alg = Metropolis() if alg is None else alg
+    if not isinstance(alg, _Alg):
+        raise NotImplementedError("alg must be Metropolis(), MetropolisAdaptive() or MetropolisFixedCone()")
+    if len(set(mc.temperatures.tolist())) != 1:
+        raise ValueError("simulated_annealing needs one target temperature for all replicas")
+    temps = annealing_temperatures(schedule, T0, float(mc.temperatures[0]))
+    p = mc.parameters
+    R = mc.n_replicas
+    acc = np.zeros((len(temps), R))
+    if temps:
+        t = np.asarray(temps, dtype=np.float64)
+        mc.ctx.call("csmc_anneal", _lib.ptr(t, C.c_double), len(temps), p.t_thermalization,
+                    p.overrelaxation_rate, alg.kind, C.c_double(mc.sigma0), _PATHS[mc.path], _lib.ptr(acc, C.c_double))
+    if verbose:
+        total = p.t_thermalization * mc.lattice.size / (p.overrelaxation_rate or 1)
+        for T, a in zip(temps, acc[:, 0]):
+            print(f"Acceptance rate at T={T}: {round(a / total * 100, 5)} % ")
+    mc.sync()
+    return acc
+
+
+def deterministic_updates(mc: MonteCarlo) -> None:
+    """deterministic_updates! (monte_carlo.jl:201-213).
+
+    The reference makes t_deterministic-1 single-site updates at random sites;
+    here they are ceil((t_deterministic-1)/N) colour sweeps, every site once
+    per sweep.
+    """
+    n = max(mc.parameters.t_deterministic - 1, 0)
+    sweeps = -(-n // mc.lattice.size)
+    mc.ctx.call("csmc_deterministic_sweeps", int(sweeps))
+    mc.sync()
+
+
+def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbose: bool = True,
+                       resident_block: int = 0) -> dict:
+    """parallel_tempering! (monte_carlo.jl:235-398) with the ranks as replicas on one GPU.
+
+    Like the reference, report_interval and checkpoint_rate must be nonzero
+    (``sweep % 0`` throws a DivideError at monte_carlo.jl:355 and :383).
+    Returns the per-replica energy and |M| series and the derived observables.
+    """
+    alg = Metropolis() if alg is None else alg
+    if not isinstance(alg, _Alg):
+        raise NotImplementedError("alg must be Metropolis(), MetropolisAdaptive() or MetropolisFixedCone()")
+    p = mc.parameters
+    if p.report_interval == 0:
+        raise ZeroDivisionError("integer division error: report_interval is 0 (monte_carlo.jl:383)")
+    if p.checkpoint_rate == 0 and p.t_measurement > 0:
+        raise ZeroDivisionError("integer division error: checkpoint_rate is 0 (monte_carlo.jl:355)")
+    R = mc.n_replicas
+    if R == 1 and verbose:
+        warnings.warn("MPI commSize of 1; no replica exchanges will occur!")
+    total = p.t_thermalization + p.t_measurement
+    Es, Ms = [], []
+    start = 0
+    while start < total:
+        n = min(p.report_interval, total - start)
+        cap = n // max(p.probe_rate, 1) + 2
+        rec_E = np.zeros((cap, R))
+        rec_M = np.zeros((cap, R))
+        acc = np.zeros(R)
+        exc = np.zeros(R)
+        rp = _lib.RunParams()
+        rp.sweep_start = start
+        rp.n_sweeps = n
+        rp.t_thermalization = p.t_thermalization
+        rp.overrelaxation_rate = p.overrelaxation_rate
+        rp.swap_rate = p.swap_rate if R > 1 else 0
+        rp.probe_rate = p.probe_rate
+        rp.kind = alg.kind
+        rp.path = _PATHS[mc.path]
+        rp.resident_block = resident_block
+        rp.probe_energy = _lib.ptr(rec_E, C.c_double)
+        rp.probe_magnetization = _lib.ptr(rec_M, C.c_double)
+        rp.probe_capacity = cap
+        rp.accepted = _lib.ptr(acc, C.c_double)
+        rp.exchanged = _lib.ptr(exc, C.c_double)
+        mc.ctx.call("csmc_run", C.byref(rp))
+        k = rp.n_probes_out
+        Es.append(rec_E[:k])
+        Ms.append(rec_M[:k])
+        mc.accepted += acc
+        mc.exchanged += exc
+        start += n
+        if verbose:
+            _print_runtime_statistics(mc, start, acc, exc, n)
+    E = np.concatenate(Es) if Es else np.zeros((0, R))
+    M = np.concatenate(Ms) if Ms else np.zeros((0, R))
+    for r in range(R):
+        for e, m in zip(E[:, r], M[:, r]):
+            mc.observables[r].push(e, m)
+    mc.sync()
+    return {"energy": E, "magnetization": M, "summary": summarize(mc, E, M)}
+
+
+def _print_runtime_statistics(mc, t, acc, exc, n):
+    """print_runtime_statistics! (helper.jl:25-78), one line per replica."""
+    p = mc.parameters
+    total = p.t_thermalization + p.t_measurement
+    attempted = n * mc.lattice.size / (p.overrelaxation_rate or 1)
+    lines = [f"Sweep {t} / {total} ({100.0 * t / total:.1f}%)",
+             f"\t\tthermalized : {'YES' if t >= p.t_thermalization else 'NO'}"]
+    sig = np.atleast_1d(mc.sigma)
+    for r in range(mc.n_replicas):
+        lines.append(f"\t\tsimulation {r} update acceptance rate : {acc[r] / attempted * 100:.2f}%\tsigma : "
+                     f"{sig[r]:.2f}")
+        if mc.n_replicas > 1 and p.swap_rate > 0:
+            att = n / p.swap_rate / (2.0 if r in (0, mc.n_replicas - 1) else 1.0)
+            lines.append(f"\t\tsimulation {r} replica exchange acceptance rate : {exc[r] / att * 100:.2f}%")
+    print("\n".join(lines) + "\n")
+
+
+def summarize(mc: MonteCarlo, E: np.ndarray, M: np.ndarray) -> list[dict]:
+    """write_final_observables content (hdf5.jl:204-239) per replica, without the file."""
+    out = []
+    N = mc.lattice.size
+    for r in range(mc.n_replicas):
+        T = float(mc.temperatures[r])
+        e, de = mean_and_error(E[:, r]) if len(E) else (float("nan"), float("nan"))
+        m, dm = mean_and_error(M[:, r]) if len(M) else (float("nan"), float("nan"))
+        c, dc = specific_heat(E[:, r], T, N) if len(E) else (float("nan"), float("nan"))
+        x, dx = susceptibility(M[:, r], T, N) if len(M) else (float("nan"), float("nan"))
+        out.append(dict(T=T, energy=e, energy_err=de, magnetization=m, magnetization_err=dm,
+                        specific_heat=c, specific_heat_err=dc, susceptibility=x, susceptibility_err=dx))
+    return out
+
+
+def replay(mc: MonteCarlo, sites, u_phi, u_z, u_acc, alg: _Alg | None = None, T=None, slot: int = 0):
+    """Replay of one reference Metropolis sweep's proposals (0-based sites and uniforms), FP64."""
+    alg = Metropolis() if alg is None else alg
+    n = len(sites)
+    s = np.ascontiguousarray(sites, dtype=np.int64)
+    up, uz, ua = (np.ascontiguousarray(a, dtype=np.float64) for a in (u_phi, u_z, u_acc))
+    acc = np.zeros(n, np.uint8)
+    sig = C.c_double(float(np.atleast_1d(mc.sigma)[slot]))
+    T = float(mc.temperatures[slot]) if T is None else float(T)
+    mc.ctx.call("csmc_replay", int(slot), alg.kind, C.c_double(T), C.byref(sig), n, _lib.ptr(s, C.c_int64),
+                _lib.ptr(up, C.c_double), _lib.ptr(uz, C.c_double), _lib.ptr(ua, C.c_double),
+                _lib.ptr(acc, C.c_uint8))
+    return acc, sig.value

@@ -1,0 +1,259 @@
+/*
+ * csmc.h -- C ABI of libcsmc.so, the GB300 (sm_103a) Monte Carlo sweep
+ * library for classical spin Hamiltonians with Zeeman, onsite, bilinear,
+ * cubic and quartic terms on Bravais lattices with a basis.
+ *
+ * This is the boundary a host binding (Julia `ccall`, Python `ctypes`, C/C++)
+ * calls in place of the sweep routines of ClassicalSpinMC.jl v1.0.0.  Every
+ * entry point names the reference routine it replaces (file:line within the
+ * ClassicalSpinMC.jl project).  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every function returns CSMC_OK (0) or a CSMC_ERR_* code and never aborts;
+ *    csmc_last_error() returns the calling thread's last message.
+ *  - Spin arrays on the host use the reference layout: the 3 x N column-major
+ *    Float64 array `lattice.spins` (lattice.jl:73), i.e. x,y,z interleaved per
+ *    site, sites in the reference's order (basis slowest, last lattice
+ *    dimension fastest; lattice.jl:29-33).
+ *  - A context holds one or more lattices ("systems"), each with R replicas.
+ *    Replica r of a system is temperature slot r: the MPI rank r of the
+ *    reference's parallel tempering (monte_carlo.jl:246-259).  Exchanges swap
+ *    which configuration sits in which slot; all per-replica inputs and
+ *    outputs of this API are indexed by slot, in system order (slot index =
+ *    sum of the replica counts of the earlier systems + r).
+ *  - Host buffers are borrowed for the duration of the call.  Device memory
+ *    is owned by the context.  One host thread per context at a time.
+ *  - Basis indices in csmc_lattice_desc are 1-based, as in the reference API.
+ */
+#ifndef CSMC_H
+#define CSMC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CSMC_OK 0
+#define CSMC_ERR_INVALID 1     /* bad argument or lattice description */
+#define CSMC_ERR_OOM 2         /* device or host allocation failed */
+#define CSMC_ERR_CUDA 3        /* CUDA runtime error (no device, launch failure, ...) */
+#define CSMC_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define CSMC_ERR_COLOURING 5   /* no valid colouring within CSMC_MAX_COLOURS */
+#define CSMC_ERR_UNSUPPORTED 6 /* description valid for the reference, not for these kernels */
+
+#define CSMC_MAX_COLOURS 16
+
+/* precision of a context */
+#define CSMC_FP64 0 /* spins, fields and dE in Float64 */
+#define CSMC_FP32 1 /* spins, fields and dE in Float32; energies, swap exponent and
+                       observable accumulators in Float64 */
+
+/* Metropolis sweep kinds: the FunctionWrapper constructors of metropolis.jl:181-199 */
+#define CSMC_METROPOLIS 0           /* Metropolis()          -> metropolis!            :65-82   */
+#define CSMC_METROPOLIS_ADAPTIVE 1  /* MetropolisAdaptive()  -> metropolis_adaptive!   :113-133 */
+#define CSMC_METROPOLIS_FIXED_CONE 2 /* MetropolisFixedCone() -> metropolis_fixed_cone! :136-153 */
+
+/* execution path of the multi-sweep drivers */
+#define CSMC_PATH_AUTO 0
+#define CSMC_PATH_RESIDENT 1 /* persistent kernel, each replica held in shared memory */
+#define CSMC_PATH_GLOBAL 2   /* one launch per colour class per sweep, all replicas batched */
+#define CSMC_PATH_PER_REPLICA 3 /* like GLOBAL but one replica per launch ("plain" path) */
+
+/* The arguments of `Lattice(shape, uc, S; bc)` (lattice.jl:65-66) with the
+ * term lists of the UnitCell (unit_cell.jl:3-18, addZeemanCoupling! :30-32,
+ * addOnSite! :37-41, addBilinear! :46-52, addCubic! :57-63, addQuartic! :68-75).
+ * Matrices are row-major (m[a*3+b] = M[a,b]); cubic tensors t[(a*3+b)*3+c] =
+ * C[a,b,c]; quartic t[((a*3+b)*3+c)*3+d] = R[a,b,c,d].  Offsets hold `dim`
+ * ints per vector: bilinear one per term, cubic two (o2, o3), quartic three
+ * (o2, o3, o4). */
+typedef struct {
+    int32_t dim;          /* D = 1, 2 or 3 */
+    int32_t n_basis;      /* 0 is treated as one basis site (lattice.jl:68-70) */
+    int32_t shape[3];     /* lattice extent per dimension (first `dim` used) */
+    int32_t periodic;     /* 1: bc="periodic", 0: bc="open" */
+    double spin_length;   /* S */
+    int32_t n_field;
+    const int32_t *field_basis;
+    const double *field_vec;
+    int32_t n_onsite;
+    const int32_t *onsite_basis;
+    const double *onsite_mat;
+    int32_t n_bilinear;
+    const int32_t *bilinear_basis; /* 2 per term */
+    const double *bilinear_mat;    /* 9 per term */
+    const int32_t *bilinear_offset;
+    int32_t n_cubic;
+    const int32_t *cubic_basis;    /* 3 per term */
+    const double *cubic_tensor;    /* 27 per term */
+    const int32_t *cubic_offset;
+    int32_t n_quartic;
+    const int32_t *quartic_basis;  /* 4 per term */
+    const double *quartic_tensor;  /* 81 per term */
+    const int32_t *quartic_offset;
+} csmc_lattice_desc;
+
+/* Summary of the flattened interaction tables of one lattice. */
+typedef struct {
+    int64_t n_sites;        /* N = prod(shape) * n_basis */
+    int32_t n_colours;      /* colour classes of the interaction hypergraph */
+    int32_t n_bilinear;     /* N2, N3, N4: the reference's per-site tuple lengths */
+    int32_t n_cubic;
+    int32_t n_quartic;
+    int32_t width_bilinear; /* non-self bilinear slots per site in the device tables */
+    int32_t width_cubic;
+    int32_t width_quartic;
+    int32_t n_matrices;     /* distinct 3x3 couplings after deduplication */
+    int32_t n_cubic_tensors;
+    int32_t n_quartic_tensors;
+    int64_t padded_sites;   /* device length of one replica (colour classes padded) */
+} csmc_lattice_info;
+
+/* Parameters of a multi-sweep run: the loop of parallel_tempering!
+ * (monte_carlo.jl:288-388).  Iterations i = sweep_start .. sweep_start+n_sweeps-1
+ * each run, in order: an overrelaxation sweep (if overrelaxation_rate != 0);
+ * if i % max(overrelaxation_rate,1) == 0 a Metropolis sweep, the total energy,
+ * and if i % swap_rate == 0 a replica exchange between neighbouring slots;
+ * then, if i >= t_thermalization and i % probe_rate == 0, a probe recording
+ * each slot's energy (from its last Metropolis sweep) and |M|. */
+typedef struct {
+    int64_t sweep_start;
+    int64_t n_sweeps;
+    int64_t t_thermalization;
+    int32_t overrelaxation_rate;
+    int32_t swap_rate;        /* <= 0: no exchanges */
+    int32_t probe_rate;       /* <= 0: no probes */
+    int32_t kind;             /* CSMC_METROPOLIS* */
+    int32_t path;             /* CSMC_PATH_* */
+    int32_t resident_block;   /* threads per CTA of the resident kernel: 256, 512, 1024; 0 = 512 */
+    double *probe_energy;     /* [probe_capacity][n_slots] or NULL */
+    double *probe_magnetization; /* [probe_capacity][n_slots] or NULL */
+    int64_t probe_capacity;
+    double *accepted;         /* [n_slots] accepted Metropolis proposals added, or NULL */
+    double *exchanged;        /* [n_slots] accepted exchanges added, or NULL */
+    int64_t n_probes_out;     /* set: probes recorded by this call */
+} csmc_run_params;
+
+/* ---------------------------------------------------------------- errors */
+const char *csmc_last_error(void);
+const char *csmc_version(void);
+
+/* ------------------------------------------------ tables (host only, no GPU) */
+
+/* Flatten and colour a lattice; replaces the table build of Lattice()
+ * (lattice.jl:65-291) with arithmetic neighbour lookup instead of findfirst. */
+int csmc_lattice_plan(const csmc_lattice_desc *desc, csmc_lattice_info *info);
+
+/* Export the per-site tables in the layout of the Lattice struct
+ * (lattice.jl:15-22): 1-based neighbour indices, 0 = absent, zero matrices
+ * where the site plays no role.  Shapes as csmc_lattice_info's n_sites and
+ * N2/N3/N4: bil_sites N*N2, bil_mats N*N2*9, cub_sites N*N3*2, cub_tens
+ * N*N3*27, qua_sites N*N4*3, qua_tens N*N4*81, field N*3, onsite N*9.  Any
+ * pointer may be NULL. */
+int csmc_lattice_tables(const csmc_lattice_desc *desc, int64_t *bil_sites, double *bil_mats,
+                        int64_t *cub_sites, double *cub_tens, int64_t *qua_sites,
+                        double *qua_tens, double *field, double *onsite);
+
+/* Colour of every site (reference order) and the device order: for device
+ * position d < padded_sites, ref_of_device[d] is the 0-based reference site or
+ * -1 for padding.  colour_start[c] is the first device position of colour c.
+ * Any pointer may be NULL. */
+int csmc_lattice_colouring(const csmc_lattice_desc *desc, int32_t *colour_of_site,
+                           int64_t *ref_of_device, int64_t *colour_start);
+
+/* ---------------------------------------------------------------- context */
+
+/* Device half of MonteCarlo(T, lattice, params) (monte_carlo.jl:56-118) for
+ * n_replicas temperature slots of one lattice.  Spins start at zero; call
+ * csmc_random_spins or csmc_set_spins.  seed keys the Philox4x32-10 streams. */
+int csmc_create(const csmc_lattice_desc *desc, int32_t precision, int32_t n_replicas,
+                uint64_t seed, void **ctx_out);
+/* Several lattices in one context, e.g. independent chains of different sizes. */
+int csmc_create_batch(const csmc_lattice_desc *descs, int32_t n_lattices,
+                      const int32_t *replicas_per_lattice, int32_t precision, uint64_t seed,
+                      void **ctx_out);
+int csmc_destroy(void *ctx);
+
+int csmc_num_slots(void *ctx, int32_t *n_slots);
+int csmc_lattice_info_of(void *ctx, int32_t lattice, csmc_lattice_info *info);
+
+/* lattice.spins of one slot, reference layout (lattice.jl:293-301). */
+int csmc_set_spins(void *ctx, int32_t slot, const double *spins);
+int csmc_get_spins(void *ctx, int32_t slot, double *spins);
+/* All slots, concatenated in slot order. */
+int csmc_set_spins_all(void *ctx, const double *spins);
+int csmc_get_spins_all(void *ctx, double *spins);
+/* Uniform random spins of length S from the Philox INIT stream
+ * (Lattice initialCondition=:random, lattice.jl:76-79). */
+int csmc_random_spins(void *ctx, uint64_t seed);
+
+/* mc.T per slot (monte_carlo.jl:72); also resets the slot permutation. */
+int csmc_set_temperatures(void *ctx, const double *T);
+/* mc.sigma per slot (monte_carlo.jl:79, metropolis.jl:84-87). */
+int csmc_set_sigma(void *ctx, const double *sigma);
+int csmc_get_sigma(void *ctx, double *sigma);
+/* For each slot, the physical replica whose spins sit there. */
+int csmc_get_permutation(void *ctx, int32_t *replica_of_slot);
+
+/* ------------------------------------------------------------ hot path */
+
+/* get_local_field (hamiltonian.jl:3-67) at every site of one slot; H is 3 x N
+ * in the reference layout. */
+int csmc_local_field(void *ctx, int32_t slot, double *H);
+/* calculate_energy_diff! (metropolis.jl:94-110) without mutation: for n
+ * proposals (0-based reference sites, new spins 3 per proposal), the energy
+ * change of moving that one site, all else fixed. */
+int csmc_energy_diff(void *ctx, int32_t slot, int64_t n, const int64_t *sites,
+                     const double *new_spins, double *dE);
+/* total_energy (hamiltonian.jl:70-132), one per slot. */
+int csmc_total_energy(void *ctx, double *E);
+/* get_magnetization (observables.jl:12-18): |sum_i s_i|, one per slot. */
+int csmc_magnetization(void *ctx, double *M);
+
+/* alg(mc, T): one Metropolis sweep on every slot at its temperature
+ * (metropolis.jl:65-153).  The sweep visits every site once, colour class by
+ * colour class.  accepted[n_slots] (or NULL) receives the accepted count. */
+int csmc_metropolis_sweep(void *ctx, int32_t kind, double *accepted);
+/* overrelaxation! (monte_carlo.jl:126-139) on every slot. */
+int csmc_overrelax_sweep(void *ctx);
+/* deterministic_updates! (monte_carlo.jl:201-213) as n_sweeps colour sweeps
+ * of s_i <- -S H_i/|H_i| on every slot. */
+int csmc_deterministic_sweeps(void *ctx, int64_t n_sweeps);
+
+/* Replay of metropolis!/metropolis_adaptive!/metropolis_fixed_cone!
+ * (metropolis.jl:65-153) on one slot, fed with the reference's proposals: n
+ * 0-based sites and uniforms.  u_acc[p] is used only where dE >= 0.  FP64,
+ * sequential, the reference's evaluation order without FMA contraction.
+ * sigma is read (cone kinds) and, for the adaptive kind, updated. */
+int csmc_replay(void *ctx, int32_t slot, int32_t kind, double T, double *sigma, int64_t n,
+                const int64_t *sites, const double *u_phi, const double *u_z,
+                const double *u_acc, uint8_t *accepted);
+
+/* The sweep loop of parallel_tempering! (monte_carlo.jl:288-388), every slot
+ * at its temperature, exchanges on the device (monte_carlo.jl:308-349). */
+int csmc_run(void *ctx, csmc_run_params *params);
+
+/* simulated_annealing! (monte_carlo.jl:157-190) on every slot: for each of the
+ * n_temps temperatures, sigma reset to sigma0, then t_thermalization-1
+ * iterations of [overrelaxation, Metropolis every overrelaxation_rate-th].
+ * accepted[n_temps * n_slots] or NULL. */
+int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_thermalization,
+                int32_t overrelaxation_rate, int32_t kind, double sigma0, int32_t path,
+                double *accepted);
+
+/* Spin-length renormalisation interval of the single-precision kernels, in
+ * sweeps (0 = never).  Default 64. */
+int csmc_set_renormalize(void *ctx, int32_t every_sweeps);
+/* max over sites and slots of ||s_i| - S| / S. */
+int csmc_spin_length_drift(void *ctx, double *drift);
+
+/* Device time (CUDA events on the context's stream) of the last csmc_run /
+ * csmc_anneal call and the number of kernel launches it issued; of those, the
+ * summed time and count of the resident sweep-kernel launches. */
+int csmc_last_run_stats(void *ctx, double *device_ms, int64_t *launches, double *sweep_kernel_ms,
+                        int64_t *sweep_kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
