@@ -88,6 +88,7 @@ SIGNATURES = {
     "csmc_get_permutation": (C.c_int, [_vp, i32p]),
     "csmc_local_field": (C.c_int, [_vp, C.c_int32, f64p]),
     "csmc_energy_diff": (C.c_int, [_vp, C.c_int32, C.c_int64, i64p, f64p, f64p]),
+    "csmc_energy_diff_static": (C.c_int, [_vp, C.c_int32, C.c_int64, i64p, f64p, f64p]),
     "csmc_total_energy": (C.c_int, [_vp, f64p]),
     "csmc_magnetization": (C.c_int, [_vp, f64p]),
     "csmc_metropolis_sweep": (C.c_int, [_vp, C.c_int32, f64p]),

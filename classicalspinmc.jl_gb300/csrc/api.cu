@@ -1049,6 +1049,50 @@ int csmc_energy_diff(void *c, int32_t slot, int64_t n, const int64_t *sites, con
     API_END
 }
 
+} // extern "C"
+
+namespace csmc {
+
+void set_last_error(const char *msg) { g_err = msg; }
+
+int context_device(void *c, int *device) {
+    API_BEGIN
+    require(device != nullptr, CSMC_ERR_INVALID, "device is NULL");
+    *device = ctx_of(c).device;
+    API_END
+}
+
+// csmc_energy_diff staged through caller-provided device memory (`scratch`,
+// laid out as n_max sites | 3*n_max new spins | n_max results): no device
+// or host allocation on the success path.
+int energy_diff_staged(void *c, int32_t slot, int64_t n, const int64_t *sites, const double *ns, double *dE,
+                       void *scratch, int64_t n_max) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(n >= 0 && n <= n_max, CSMC_ERR_INVALID, "n outside 0..capacity");
+    require(n == 0 || (sites && ns && dE), CSMC_ERR_INVALID, "NULL argument");
+    System &S = *C.sys[C.sys_of_slot(slot)];
+    for (int64_t q = 0; q < n; q++)
+        require(sites[q] >= 0 && sites[q] < S.plan.N, CSMC_ERR_INVALID, "site index out of range");
+    if (n == 0) return CSMC_OK;
+    int32_t chain = 0;
+    CK(cudaMemcpy(&chain, C.chain_of.p + slot, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    const int r = chain - S.base;
+    int64_t *d_sites = static_cast<int64_t *>(scratch);
+    double *d_ns = reinterpret_cast<double *>(d_sites + n_max);
+    double *d_dE = d_ns + 3 * n_max;
+    CK(cudaMemcpyAsync(d_sites, sites, n * sizeof(int64_t), cudaMemcpyHostToDevice, C.st));
+    CK(cudaMemcpyAsync(d_ns, ns, 3 * n * sizeof(double), cudaMemcpyHostToDevice, C.st));
+    with_args(C, S, [&](auto &a) { launch_energy_diff(a, r, n, d_sites, d_ns, d_dE, C.st); });
+    CK(cudaMemcpyAsync(dE, d_dE, n * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    sync_check(C);
+    API_END
+}
+
+} // namespace csmc
+
+extern "C" {
+
 int csmc_total_energy(void *c, double *E) {
     API_BEGIN
     Ctx &C = ctx_of(c);

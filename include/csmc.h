@@ -205,6 +205,20 @@ int csmc_local_field(void *ctx, int32_t slot, double *H);
  * change of moving that one site, all else fixed. */
 int csmc_energy_diff(void *ctx, int32_t slot, int64_t n, const int64_t *sites,
                      const double *new_spins, double *dE);
+/* The same energy differences as csmc_energy_diff, with no device allocation.
+ * No counterpart in the reference.  csmc_energy_diff allocates and frees its
+ * device staging on every call; callers whose memory pool already holds the
+ * GPU's memory, or whose proposal loop cannot afford the synchronising
+ * cudaFree, use this one: it stages through a 2.5 MiB static device array
+ * compiled into the library (held on every GPU that loads it until exit).
+ * n may not exceed CSMC_ENERGY_DIFF_STATIC_MAX (CSMC_ERR_INVALID otherwise).
+ * The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  All calls share the array and
+ * it keeps the last call's contents (nothing in it needs to start at zero);
+ * calls whose GPU work overlaps race on it and must be serialised. */
+#define CSMC_ENERGY_DIFF_STATIC_MAX 65536
+int csmc_energy_diff_static(void *ctx, int32_t slot, int64_t n, const int64_t *sites,
+                            const double *new_spins, double *dE);
 /* total_energy (hamiltonian.jl:70-132), one per slot. */
 int csmc_total_energy(void *ctx, double *E);
 /* get_magnetization (observables.jl:12-18): |sum_i s_i|, one per slot. */
