@@ -51,6 +51,7 @@ L_SIDE, R_REPL, OR_RATE, SWAP_RATE, PROBE_RATE = 24, 64, 5, 10, 10
 ITER_PER_STEP = 10
 SEED = 20261203
 BYTES_PER_UPDATE_FP32 = 12 * (2 + 6)  # s_b * (2 + z): own spin read+write, 6 neighbours read
+RESIDENT_BLOCK = 0
 
 
 def workload_config(extra=None):
@@ -126,6 +127,7 @@ def run_params(L, start, n, rec_E=None, rec_M=None, cap=0, path=0):
     rp.probe_rate = PROBE_RATE
     rp.kind = L.METROPOLIS
     rp.path = path
+    rp.resident_block = RESIDENT_BLOCK
     if rec_E is not None:
         rp.probe_energy = rec_E.ctypes.data_as(C.POINTER(C.c_double))
         rp.probe_magnetization = rec_M.ctypes.data_as(C.POINTER(C.c_double))
@@ -274,7 +276,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
     args = ap.parse_args()
+    global RESIDENT_BLOCK
+    RESIDENT_BLOCK = args.block
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     threads = os.cpu_count() or 1

@@ -63,11 +63,16 @@ struct System {
     DevBuf<uint8_t> pat;
     DevBuf<int32_t> dev2ref, c2, c3, c4;
     DevBuf<int64_t> ref2dev;
-    DevBuf<float> fmats, fcubs, fquas, fO, fP, fh, fspins;
-    DevBuf<double> dmats, dcubs, dquas, dO, dP, dh, dspins;
+    DevBuf<float> fmats, fcubs, fquas, fO, fP, fh, fspins, fA, fQ, fE2, fJs;
+    DevBuf<double> dmats, dcubs, dquas, dO, dP, dh, dspins, dA, dQ, dE2, dJs;
     SysArgs<float> fa{};
     SysArgs<double> da{};
     bool resident_ok = false;
+    // specialised resident kernel: eligible, bilinear and onsite classes, and
+    // the single basis of each colour class
+    bool fast_ok = false;
+    int bil_class = 1, ons_class = 2;
+    std::vector<int32_t> col_pattern;
     size_t resident_smem = 0;
     // reference-layout tables for the replay kernel (built on first use)
     DevBuf<int64_t> xbs, xcs, xqs;
@@ -168,6 +173,42 @@ static void upload_system(Ctx &C, System &S) {
     }
     S.cub = P.W3 > 0;
     S.qua = P.W4 > 0;
+    // per pattern: 2O+P (local field), O+P (dE), O+P/2 (energy share)
+    std::vector<double> A((nb + 1) * 9, 0.0), Qm((nb + 1) * 9, 0.0), E2((nb + 1) * 9, 0.0);
+    for (int k = 0; k < (nb + 1) * 9; k++) {
+        A[k] = 2 * O[k] + Pm[k];
+        Qm[k] = O[k] + Pm[k];
+        E2[k] = O[k] + 0.5 * Pm[k];
+    }
+    S.ons_class = 0;
+    for (int b = 0; b <= nb; b++)
+        for (int k = 0; k < 9; k++) {
+            const bool diag = k == 0 || k == 4 || k == 8;
+            if (A[b * 9 + k] != 0.0 || Qm[b * 9 + k] != 0.0) S.ons_class = std::max(S.ons_class, diag ? 1 : 2);
+        }
+    // scalar couplings: every bilinear slot matrix is c * I
+    const int W2 = std::max(P.W2, 1);
+    std::vector<double> Js((size_t)(nb + 1) * W2, 0.0);
+    S.bil_class = 0;
+    for (int b = 0; b < nb; b++)
+        for (int t = 0; t < P.W2; t++) {
+            const double *M = &P.mats[9 * (size_t)P.c2[(size_t)b * P.W2 + t]];
+            const bool scalar = M[1] == 0 && M[2] == 0 && M[3] == 0 && M[5] == 0 && M[6] == 0 && M[7] == 0 &&
+                                M[0] == M[4] && M[4] == M[8];
+            if (!scalar) S.bil_class = 1;
+            Js[(size_t)b * W2 + t] = M[0];
+        }
+    S.col_pattern.assign(P.n_colours, -1);
+    bool uniform = true;
+    for (int col = 0; col < P.n_colours; col++) {
+        int pb = -1;
+        for (int64_t d = P.col_start[col]; d < P.col_start[col] + P.col_count[col]; d++) {
+            if (pb < 0) pb = P.pat[d];
+            if (P.pat[d] != pb) uniform = false;
+        }
+        S.col_pattern[col] = pb < 0 ? nb : pb;
+    }
+    S.fast_ok = uniform && !S.cub && !S.qua && P.W2 <= RESIDENT_WMAX;
     const int64_t Np = P.Np;
     if (P.Np <= 65536) {
         std::vector<uint16_t> a(P.p2.begin(), P.p2.end()), b(P.p3.begin(), P.p3.end()), c(P.p4.begin(), P.p4.end());
@@ -215,6 +256,14 @@ static void upload_system(Ctx &C, System &S) {
         S.fspins.alloc(nsp);
         CK(cudaMemset(S.fspins.p, 0, nsp * sizeof(float)));
         fill_args(S.fa, S.fspins.p, S.fmats.p, S.fcubs.p, S.fquas.p, S.fO.p, S.fP.p, S.fh.p);
+        S.fA.upload(to_f(A));
+        S.fQ.upload(to_f(Qm));
+        S.fE2.upload(to_f(E2));
+        S.fJs.upload(to_f(Js));
+        S.fa.cf.A = S.fA.p;
+        S.fa.cf.Q = S.fQ.p;
+        S.fa.cf.E2 = S.fE2.p;
+        S.fa.cf.Js = S.fJs.p;
         S.fa.S = (float)P.desc.S;
         S.resident_smem = 3 * Np * sizeof(float);
     } else {
@@ -227,10 +276,20 @@ static void upload_system(Ctx &C, System &S) {
         S.dspins.alloc(nsp);
         CK(cudaMemset(S.dspins.p, 0, nsp * sizeof(double)));
         fill_args(S.da, S.dspins.p, S.dmats.p, S.dcubs.p, S.dquas.p, S.dO.p, S.dP.p, S.dh.p);
+        S.dA.upload(A);
+        S.dQ.upload(Qm);
+        S.dE2.upload(E2);
+        S.dJs.upload(Js);
+        S.da.cf.A = S.dA.p;
+        S.da.cf.Q = S.dQ.p;
+        S.da.cf.E2 = S.dE2.p;
+        S.da.cf.Js = S.dJs.p;
         S.da.S = P.desc.S;
         S.resident_smem = 3 * Np * sizeof(double);
     }
-    S.resident_ok = P.Np <= 65536 && (int64_t)S.resident_smem <= (int64_t)C.max_smem - 1024 &&
+    // dynamic shared memory holds the replica; keep 12 KB for the kernel's
+    // static shared memory (descriptor, reduction scratch, staged couplings)
+    S.resident_ok = P.Np <= 65536 && (int64_t)S.resident_smem <= (int64_t)C.max_smem - 12 * 1024 &&
                     P.n_colours <= CSMC_MAX_COLOURS;
 }
 
@@ -252,6 +311,7 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     r.nb = S.plan.desc.nb;
     for (int c = 0; c <= S.plan.n_colours; c++) r.col_start[c] = S.plan.col_start[c];
     for (int c = 0; c < S.plan.n_colours; c++) r.col_count[c] = S.plan.col_count[c];
+    for (int c = 0; c < S.plan.n_colours; c++) r.col_pattern[c] = S.col_pattern[c];
     r.n_real = S.plan.N;
     r.S = a.S;
     r.k0 = a.k0;
@@ -540,21 +600,36 @@ static int choose_path(Ctx &C, int requested) {
     return all ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
 }
 
+static ResidentSel resident_selection(const Ctx &C);
+
+// 512 or 1024 threads per CTA; by default 1024 for the specialised kernel
+// (fits 64 registers) and 512 for the generic one (needs more registers).
 static int resident_block(Ctx &C, int hint) {
-    if (hint == 256 || hint == 512 || hint == 1024) return hint;
-    return 512;
+    if (hint == 512 || hint == 1024) return hint;
+    return resident_selection(C).fast ? 1024 : 512;
+}
+
+// The resident kernel for every lattice of the context: the specialised one
+// when all lattices allow it (with the widest coupling classes among them),
+// else the generic one.
+static ResidentSel resident_selection(const Ctx &C) {
+    ResidentSel sel{true, 0, 0, false, false};
+    for (auto &S : C.sys) {
+        sel.fast = sel.fast && S->fast_ok;
+        sel.bil = std::max(sel.bil, S->bil_class);
+        sel.ons = std::max(sel.ons, S->ons_class);
+        sel.cub = sel.cub || S->cub;
+        sel.qua = sel.qua || S->qua;
+    }
+    return sel;
 }
 
 static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
     size_t smem = 0;
-    bool cub = false, qua = false;
-    for (auto &S : C.sys) {
-        smem = std::max(smem, S->resident_smem);
-        cub = cub || S->cub;
-        qua = qua || S->qua;
-    }
-    int per_sm = C.precision == CSMC_FP32 ? resident_max_blocks_per_sm<float>(block, smem, cub, qua)
-                                          : resident_max_blocks_per_sm<double>(block, smem, cub, qua);
+    for (auto &S : C.sys) smem = std::max(smem, S->resident_smem);
+    const ResidentSel sel = resident_selection(C);
+    int per_sm = C.precision == CSMC_FP32 ? resident_max_blocks_per_sm<float>(block, smem, sel)
+                                          : resident_max_blocks_per_sm<double>(block, smem, sel);
     require(per_sm >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on an SM with this shared memory size");
     const int grid = std::min(C.n_items, C.n_sms * per_sm);
     auto ev = C.next_kernel_events();
@@ -562,9 +637,9 @@ static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
     CK(cudaEventRecord(ev.first, C.st));
     cudaError_t e = C.precision == CSMC_FP32
                         ? launch_resident<float>(C.fres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid, block,
-                                                 smem, cub, qua, C.st)
+                                                 smem, sel, C.st)
                         : launch_resident<double>(C.dres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid,
-                                                  block, smem, cub, qua, C.st);
+                                                  block, smem, sel, C.st);
     CK(e);
     CK(cudaEventRecord(ev.second, C.st));
     L.n += 1;

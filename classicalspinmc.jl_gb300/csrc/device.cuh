@@ -61,6 +61,10 @@ template <typename R> struct Coef {
     const R *mats, *cubs, *quas; // deduplicated tensors, id 0 = zeros
     const R *O, *P, *h;          // per pattern: onsite (9), folded self loops (9), field (3)
     const int32_t *c2, *c3, *c4; // per pattern x slot: coefficient ids
+    // per pattern, for the specialised resident kernel: 2O+P (local field),
+    // O+P (dE), O+P/2 (energy share), and the scalar of each bilinear slot
+    // when every coupling is a multiple of the identity
+    const R *A, *Q, *E2, *Js;
 };
 
 template <typename R> struct V3 {

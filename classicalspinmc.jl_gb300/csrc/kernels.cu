@@ -1,48 +1,20 @@
-// kernels.cu -- sm_103a colour-sweep kernels for the Metropolis /
-// overrelaxation / deterministic updates, the energy and magnetisation
-// reductions and the replica exchange, in two execution forms:
-//
-//  * global path: one launch per colour class, all replicas of a lattice in
-//    the grid's y dimension (or one replica per launch for the plain path);
-//    spins live in HBM/L2, partner tables are 32-bit.
-//  * resident path: a persistent kernel, one CTA per replica, that stages
-//    the replica into shared memory with bulk TMA copies (cp.async.bulk,
-//    mbarrier completion), runs a whole window of sweeps there with
-//    __syncthreads between colour classes, and writes it back once.
+// kernels.cu -- sm_103a colour-sweep kernels of the global path: one launch
+// per colour class, all replicas of a lattice in the grid's y dimension (or
+// one replica per launch for the plain path), spins in HBM/L2, 32-bit partner
+// tables; plus the energy and magnetisation reductions, the replica exchange
+// and the layout conversions.  The persistent shared-memory kernel is in
+// resident.cuh.
 //
 // The physics per site restates hamiltonian.jl, metropolis.jl and
 // monte_carlo.jl (see device.cuh).  Colour classes make every update within
 // a class independent, so each class is one parallel step.
 #include "kernels.cuh"
 #include "launch.hpp"
+#include "reduce.cuh"
 
 namespace csmc {
 
 constexpr int GB = 256; // block size of the global-path kernels
-
-// ------------------------------------------------------------ reductions
-
-template <int NT> __device__ __forceinline__ double block_sum(double v, double *scratch) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) scratch[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < NT / 32 ? scratch[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    }
-    return t; // valid in thread 0
-}
-
-__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // ------------------------------------------------------------ global path
 
@@ -346,286 +318,6 @@ template <typename R> __global__ void k_drift(SysArgs<R> a, unsigned int *bits) 
     atomicMax(bits, __float_as_uint(e));
 }
 
-// ------------------------------------------------------------ resident path
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok)
-                 : "r"(smem_u32(bar)), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-// Bulk TMA copy global -> shared, completion counted on the mbarrier.
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// Bounded wait on an mbarrier phase: gives up after `limit` polls and
-// reports it through the context's error flag instead of hanging.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *error_flag) {
-    for (int k = 0; k < (1 << 22); k++)
-        if (mbar_try_wait(bar, parity)) return true;
-    if (threadIdx.x == 0) atomicExch(error_flag, 1);
-    return false;
-}
-
-template <typename R, bool CUB, bool QUA, int NT> struct Resident {
-    const ResSys<R> &S;
-    R *x, *y, *z;
-    double *scratch;
-    int c, slot;
-
-    __device__ __forceinline__ void barrier() const { __syncthreads(); }
-
-    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
-        unsigned acc = 0;
-        for (int col = 0; col < S.n_colours; col++) {
-            const int64_t st = S.col_start[col], n = S.col_count[col];
-            for (int64_t i = threadIdx.x; i < n; i += NT) {
-                const int64_t d = st + i;
-                const int b = S.tb.pat[d];
-                V3<R> hb, hc, hq;
-                partner_fields<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, b, hb, hc, hq);
-                const R *h = S.cf.h + 3 * b;
-                const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
-                const V3<R> s = {x[d], y[d], z[d]};
-                const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1);
-                const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
-                const R dE = delta_e<R>(S.cf, b, s, sn, hext);
-                bool accept = dE < R(0);
-                if (!accept) {
-                    const R arg = sizeof(R) == 4 ? -dE * invT : -dE / (R)T;
-                    accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
-                }
-                if (accept) {
-                    x[d] = sn.x;
-                    y[d] = sn.y;
-                    z[d] = sn.z;
-                    acc++;
-                }
-            }
-            barrier();
-        }
-        return acc;
-    }
-
-    __device__ void or_sweep() const {
-        for (int col = 0; col < S.n_colours; col++) {
-            const int64_t st = S.col_start[col], n = S.col_count[col];
-            for (int64_t i = threadIdx.x; i < n; i += NT) {
-                const int64_t d = st + i;
-                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
-                if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
-                const V3<R> s = {x[d], y[d], z[d]};
-                const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
-                x[d] = -s.x + proj * H.x;
-                y[d] = -s.y + proj * H.y;
-                z[d] = -s.z + proj * H.z;
-            }
-            barrier();
-        }
-    }
-
-    __device__ double energy() const { // valid in thread 0
-        double e = 0.0;
-        for (int col = 0; col < S.n_colours; col++) {
-            const int64_t st = S.col_start[col], n = S.col_count[col];
-            for (int64_t i = threadIdx.x; i < n; i += NT) {
-                const int64_t d = st + i;
-                e += site_energy_share<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
-            }
-        }
-        return block_sum<NT>(e, scratch);
-    }
-
-    __device__ double magnetization() const { // valid in thread 0
-        double mx = 0, my = 0, mz = 0;
-        const int64_t Np = S.tb.Np;
-        for (int64_t d = threadIdx.x; d < Np; d += NT) { // padding holds zeros
-            mx += x[d];
-            my += y[d];
-            mz += z[d];
-        }
-        mx = block_sum<NT>(mx, scratch);
-        my = block_sum<NT>(my, scratch);
-        mz = block_sum<NT>(mz, scratch);
-        return sqrt(mx * mx + my * my + mz * mz);
-    }
-
-    __device__ void renormalize() const {
-        for (int col = 0; col < S.n_colours; col++) {
-            const int64_t st = S.col_start[col], n = S.col_count[col];
-            for (int64_t i = threadIdx.x; i < n; i += NT) {
-                const int64_t d = st + i;
-                const R a = x[d], b = y[d], cc = z[d];
-                const R n2 = a * a + b * b + cc * cc;
-                if (n2 == R(0)) continue;
-                const R f = S.S * Math<R>::rsqrt_(n2);
-                x[d] = a * f;
-                y[d] = b * f;
-                z[d] = cc * f;
-            }
-        }
-        barrier();
-    }
-};
-
-// Probe of iteration q exists?  (q >= t_therm and q % probe_rate == 0)
-__device__ __forceinline__ bool is_probe(const RunDesc &rd, int64_t q) {
-    return rd.probe_rate > 0 && q >= rd.t_therm && q % rd.probe_rate == 0;
-}
-
-template <typename R, bool CUB, bool QUA, int NT>
-__global__ void __launch_bounds__(NT, 1)
-    k_resident(const ResSys<R> *__restrict__ systems, const int2 *__restrict__ items, int n_items, int *work_ctr,
-               ChainState cs, RunDesc rd) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ uint64_t bar;
-    __shared__ double scratch[32];
-    __shared__ int s_item;
-    __shared__ double s_sigma;
-    __shared__ ResSys<R> s_sys;
-    uint32_t parity = 0;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    const int64_t dosweep = rd.or_rate == 0 ? 1 : rd.or_rate;
-
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(work_ctr, 1);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= n_items) break;
-        const int2 w = items[item];
-        if (threadIdx.x == 0) s_sys = systems[w.x];
-        __syncthreads();
-        const ResSys<R> &S = s_sys;
-        const int r = w.y;
-        const int c = S.chain_base + r;
-        const int64_t Np = S.tb.Np;
-        R *gx = S.spins + (int64_t)r * 3 * Np;
-        R *x = reinterpret_cast<R *>(smem_raw), *y = x + Np, *z = y + Np;
-
-        // stage the replica: three bulk TMA copies of Np elements
-        if (threadIdx.x == 0) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const uint32_t bytes = (uint32_t)(Np * sizeof(R));
-            mbar_expect_tx(&bar, 3 * bytes);
-            bulk_g2s(x, gx, bytes, &bar);
-            bulk_g2s(y, gx + Np, bytes, &bar);
-            bulk_g2s(z, gx + 2 * Np, bytes, &bar);
-        }
-        const bool ok = mbar_wait_bounded(&bar, parity, cs.error_flag);
-        parity ^= 1;
-        if (__syncthreads_or(!ok)) { // block-uniform: wait once more for the copies in flight, drop the item
-            mbar_wait_bounded(&bar, parity ^ 1, cs.error_flag);
-            __syncthreads();
-            continue;
-        }
-
-        const int slot = cs.slot_of[c];
-        const double T = rd.T_override > 0 ? rd.T_override : cs.T_slot[slot];
-        if (threadIdx.x == 0) s_sigma = rd.reset_sigma ? rd.sigma0 : cs.sigma_slot[slot];
-        __syncthreads();
-        Resident<R, CUB, QUA, NT> k{S, x, y, z, scratch, c, slot};
-        const R invT = (R)(1.0 / T);
-        double E = cs.E_chain[c];
-        double acc_total = 0.0;
-        uint32_t msweep = rd.msweep0;
-        int sweeps_since_renorm = 0;
-
-        if (rd.pending_probe) { // probe of the exchange iteration it0-1
-            const int64_t q = rd.it0 - 1;
-            const double M = k.magnetization();
-            if (threadIdx.x == 0) {
-                const int64_t kq = (q - rd.probe_first) / rd.probe_rate;
-                if (kq >= 0 && kq < rd.probe_cap) {
-                    if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
-                    if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
-                }
-                cs.M_chain[c] = M;
-            }
-        }
-
-        for (int64_t it = rd.it0; it < rd.it1; it++) {
-            if (rd.or_rate != 0) {
-                k.or_sweep();
-                sweeps_since_renorm++;
-            }
-            const bool metro = it % dosweep == 0;
-            if (metro) {
-                const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
-                msweep++;
-                sweeps_since_renorm++;
-                const double at = block_sum<NT>((double)a, scratch);
-                if (threadIdx.x == 0) {
-                    acc_total += at;
-                    if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) {
-                        const double om = 1 - at / (double)S.n_real;
-                        const double f = 0.5 / (om > 0.05 ? om : 0.05);
-                        double sg = s_sigma * f;
-                        s_sigma = sg < 0.0 ? 0.0 : (sg > 100 ? 100 : sg);
-                    }
-                }
-                __syncthreads();
-                // energy needed: exchange point, a probe before the next
-                // Metropolis sweep, or the last Metropolis sweep of the window
-                bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-                for (int64_t q = it; q < it + dosweep && q < rd.it1 && !needE; q++) needE = is_probe(rd, q);
-                needE = needE || it + dosweep >= rd.it1;
-                if (needE) {
-                    const double e = k.energy();
-                    if (threadIdx.x == 0) E = e;
-                }
-            }
-            const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-            if (is_probe(rd, it) && !swap_here) {
-                const double M = k.magnetization();
-                if (threadIdx.x == 0) {
-                    const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
-                    if (kq >= 0 && kq < rd.probe_cap) {
-                        if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
-                        if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
-                    }
-                    cs.M_chain[c] = M;
-                }
-            }
-            if (sizeof(R) == 4 && rd.renorm_every > 0 && sweeps_since_renorm >= rd.renorm_every) {
-                k.renormalize();
-                sweeps_since_renorm = 0;
-            }
-        }
-        if (sizeof(R) == 4 && rd.renorm_every > 0 && sweeps_since_renorm > 0) k.renormalize();
-
-        if (threadIdx.x == 0) {
-            cs.E_chain[c] = E;
-            cs.acc_slot[slot] += acc_total;
-            cs.sigma_slot[slot] = s_sigma;
-        }
-        __syncthreads();
-        // write the replica back (x, y, z are contiguous in both memories)
-        for (int64_t i = threadIdx.x; i < 3 * Np; i += NT) gx[i] = x[i];
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------------------------ launchers
 
 template <typename R> static dim3 grid_for(int64_t n, int chains) {
@@ -729,39 +421,6 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
     k_drift<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, bits);
 }
 
-template <typename R, int NT> static const void *resident_fn(bool cub, bool qua) {
-    if (cub && qua) return (const void *)k_resident<R, true, true, NT>;
-    if (cub) return (const void *)k_resident<R, true, false, NT>;
-    if (qua) return (const void *)k_resident<R, false, true, NT>;
-    return (const void *)k_resident<R, false, false, NT>;
-}
-
-template <typename R>
-cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
-                            const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem, bool cub,
-                            bool qua, cudaStream_t st) {
-    const void *fn = block == 1024 ? resident_fn<R, 1024>(cub, qua)
-                     : block == 256 ? resident_fn<R, 256>(cub, qua)
-                                    : resident_fn<R, 512>(cub, qua);
-    // work_ctr must be zero when the kernel starts (the caller resets it on `st`)
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    ChainState csv = cs;
-    RunDesc rdv = rd;
-    void *args[] = {(void *)&d_sys, (void *)&items, (void *)&n_items, (void *)&work_ctr, (void *)&csv, (void *)&rdv};
-    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st);
-}
-
-template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, bool cub, bool qua) {
-    const void *fn = block == 1024 ? resident_fn<R, 1024>(cub, qua)
-                     : block == 256 ? resident_fn<R, 256>(cub, qua)
-                                    : resident_fn<R, 512>(cub, qua);
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 0;
-    return n;
-}
-
 #define INSTANTIATE(R)                                                                                                 \
     template void launch_metro_colour<R>(const SysArgs<R> &, const ChainState &, int64_t, int64_t, int, int, int,     \
                                          uint32_t, double, cudaStream_t);                                              \
@@ -776,10 +435,7 @@ template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, boo
     template void launch_energy_diff<R>(const SysArgs<R> &, int, int64_t, const int64_t *, const double *, double *,  \
                                         cudaStream_t);                                                                 \
     template void launch_renorm<R>(const SysArgs<R> &, int, int, cudaStream_t);                                       \
-    template void launch_drift<R>(const SysArgs<R> &, unsigned int *, cudaStream_t);                                  \
-    template cudaError_t launch_resident<R>(const ResSys<R> *, const int2 *, int, int *, const ChainState &,          \
-                                            const RunDesc &, int, int, size_t, bool, bool, cudaStream_t);             \
-    template int resident_max_blocks_per_sm<R>(int, size_t, bool, bool);
+    template void launch_drift<R>(const SysArgs<R> &, unsigned int *, cudaStream_t);
 
 INSTANTIATE(float)
 INSTANTIATE(double)

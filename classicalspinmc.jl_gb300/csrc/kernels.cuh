@@ -45,10 +45,23 @@ template <typename R> struct ResSys {
     int32_t n_colours, nb;
     int64_t col_start[CSMC_MAX_COLOURS + 1];
     int64_t col_count[CSMC_MAX_COLOURS];
+    int32_t col_pattern[CSMC_MAX_COLOURS]; // the one basis of each colour class, or -1
     int64_t n_real;
     R S;
     uint32_t k0, k1;
 };
+
+// Which resident kernel: the generic one (per-site pattern, cubic and
+// quartic terms) or the specialised one for lattices without cubic/quartic
+// terms whose colour classes each hold a single basis; for the latter the
+// bilinear class (0: every coupling c*I, 1: general 3x3) and the onsite class
+// (0: none, 1: diagonal, 2: general) of 2O+P.
+struct ResidentSel {
+    bool fast;
+    int bil, ons;
+    bool cub, qua;
+};
+constexpr int RESIDENT_WMAX = 8; // bilinear slots per site of the specialised kernel
 
 // The sweep schedule of one resident launch (see csmc_run_params).
 struct RunDesc {

@@ -42,9 +42,9 @@ template <typename R> void launch_renorm(const SysArgs<R> &a, int chain_lo, int 
 template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits, cudaStream_t st);
 template <typename R>
 cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
-                            const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem, bool cub,
-                            bool qua, cudaStream_t st);
-template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, bool cub, bool qua);
+                            const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem,
+                            const ResidentSel &sel, cudaStream_t st);
+template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, const ResidentSel &sel);
 
 // Reference-layout tables of one lattice for the replay kernel (exact.cu):
 // per reference site, N2/N3/N4 term entries with 0-based partners (-1 absent).

@@ -125,7 +125,7 @@ typedef struct {
     int32_t probe_rate;       /* <= 0: no probes */
     int32_t kind;             /* CSMC_METROPOLIS* */
     int32_t path;             /* CSMC_PATH_* */
-    int32_t resident_block;   /* threads per CTA of the resident kernel: 256, 512, 1024; 0 = 512 */
+    int32_t resident_block;   /* threads per CTA of the resident kernel: 512 or 1024; 0 = automatic */
     double *probe_energy;     /* [probe_capacity][n_slots] or NULL */
     double *probe_magnetization; /* [probe_capacity][n_slots] or NULL */
     int64_t probe_capacity;
