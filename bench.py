@@ -152,6 +152,10 @@ def bench_ours(args, rank, world, dist):
     ctx = m.monte_carlo.Context([lat], [R_REPL], precision="fp32", seed=SEED + rank)
     ctx.set_temperatures(temperatures())
     ctx.call("csmc_random_spins", C.c_uint64(SEED + 1000 * rank))
+    if args.cluster:
+        ctx.call("csmc_set_cluster_size", args.cluster)
+    ranks = C.c_int32()
+    ctx.call("csmc_cluster_size", C.byref(ranks))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     upd = R_REPL * lat.size * (ITER_PER_STEP + ITER_PER_STEP // OR_RATE)
     it = 1  # steps cover iterations [10k+1, 10k+10]: one exchange window each
@@ -188,7 +192,7 @@ def bench_ours(args, rank, world, dist):
         t_dev = float(tt.item())
     value = world * upd * args.steps / t_dev
     out = {"value": value, "ms_per_step": 1e3 * t_dev / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
-           "gpu_launches": launches, "clocks": clk.summary()}
+           "gpu_launches": launches, "clocks": clk.summary(), "ctas_per_replica": ranks.value}
     # roofline of the dominant kernel (the resident sweep kernel, one launch per step)
     per_launch_s = kern_ms / 1e3 / max(kern_launches, 1)
     bytes_per_launch = upd * BYTES_PER_UPDATE_FP32 * args.steps / max(kern_launches, 1)
@@ -277,6 +281,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: library default; 1, 2 or 4)")
     args = ap.parse_args()
     global RESIDENT_BLOCK
     RESIDENT_BLOCK = args.block
@@ -315,7 +320,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config({"precision": "FP32 spins/fields/dE, FP64 energies+exchange+observables",
-                                       "wall_ms_per_step": res["wall_ms_per_step"]}),
+                                       "wall_ms_per_step": res["wall_ms_per_step"],
+                                       "ctas_per_replica": res["ctas_per_replica"]}),
             "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "clocks": res["clocks"],
             "gpu_launches": res["gpu_launches"]}
     if "plain_fp64_per_replica" in res:

@@ -99,6 +99,8 @@ SIGNATURES = {
     "csmc_run": (C.c_int, [_vp, C.POINTER(RunParams)]),
     "csmc_anneal": (C.c_int, [_vp, f64p, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                               f64p]),
+    "csmc_set_cluster_size": (C.c_int, [_vp, C.c_int32]),
+    "csmc_cluster_size": (C.c_int, [_vp, i32p]),
     "csmc_set_renormalize": (C.c_int, [_vp, C.c_int32]),
     "csmc_spin_length_drift": (C.c_int, [_vp, f64p]),
     "csmc_last_run_stats": (C.c_int, [_vp, f64p, i64p, f64p, i64p]),

@@ -73,6 +73,11 @@ struct System {
     bool fast_ok = false;
     int bil_class = 1, ons_class = 2;
     std::vector<int32_t> col_pattern;
+    // split over a thread-block cluster (context-wide cluster size > 1)
+    ClusterLayout cl_layout;
+    DevBuf<uint16_t> q2c;
+    // bilinear partners packed 8 x 16 bit per site (specialised kernel)
+    DevBuf<uint4> p2v, q2v;
     size_t resident_smem = 0;
     // reference-layout tables for the replay kernel (built on first use)
     DevBuf<int64_t> xbs, xcs, xqs;
@@ -98,7 +103,9 @@ struct Ctx {
     DevBuf<ResSys<double>> dres;
     DevBuf<int2> items;
     int n_items = 0;
-    uint32_t msweep = 0;
+    int cl = 1; // CTAs per replica of the resident kernel
+    uint32_t msweep = 0;   // Metropolis sweeps so far (the Philox counter)
+    uint64_t nsweeps = 0;  // sweeps of every kind so far (renormalisation cadence)
     int renorm_every = 64;
     double last_ms = 0.0;
     int64_t last_launches = 0;
@@ -148,6 +155,19 @@ struct Ctx {
 };
 
 template <typename V> static std::vector<float> to_f(const V &v) { return std::vector<float>(v.begin(), v.end()); }
+
+// Pack a slot-major partner table [W][n] (16-bit values) into one 16-byte
+// word per site, slots >= W filled with pad(i).
+template <typename T, class Pad>
+static std::vector<uint4> pack8(const std::vector<T> &tab, int W, int64_t n, Pad pad) {
+    std::vector<uint4> out((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        uint32_t v[8];
+        for (int t = 0; t < 8; t++) v[t] = (t < W ? (uint32_t)tab[(size_t)t * n + i] : pad(i)) & 0xFFFFu;
+        out[i] = make_uint4(v[0] | v[1] << 16, v[2] | v[3] << 16, v[4] | v[5] << 16, v[6] | v[7] << 16);
+    }
+    return out;
+}
 
 static void upload_system(Ctx &C, System &S) {
     const Plan &P = S.plan;
@@ -209,6 +229,7 @@ static void upload_system(Ctx &C, System &S) {
         S.col_pattern[col] = pb < 0 ? nb : pb;
     }
     S.fast_ok = uniform && !S.cub && !S.qua && P.W2 <= RESIDENT_WMAX;
+    if (S.fast_ok && P.Np <= 65536) S.p2v.upload(pack8(P.p2, P.W2, P.Np, [&](int64_t) { return (uint32_t)P.sentinel; }));
     const int64_t Np = P.Np;
     if (P.Np <= 65536) {
         std::vector<uint16_t> a(P.p2.begin(), P.p2.end()), b(P.p3.begin(), P.p3.end()), c(P.p4.begin(), P.p4.end());
@@ -316,7 +337,111 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     r.S = a.S;
     r.k0 = a.k0;
     r.k1 = a.k1;
+    const ClusterLayout &L = S.cl_layout;
+    r.cl = L.ranks;
+    r.Npl = (int32_t)L.Npl;
+    r.q2c = S.q2c.p;
+    r.p2v = S.p2v.p;
+    r.q2v = S.q2v.p;
+    if (L.ranks > 1)
+        for (int k = 0; k < L.ranks; k++)
+            for (int c = 0; c < S.plan.n_colours; c++) {
+                r.loc_start[k][c] = (int32_t)L.loc_start[k * S.plan.n_colours + c];
+                r.loc_count[k][c] = (int32_t)L.loc_count[k * S.plan.n_colours + c];
+                r.src_start[k][c] = (int32_t)L.src_start[k * S.plan.n_colours + c];
+            }
     return r;
+}
+
+// Cluster size of the resident kernel for a context: the largest of 2 and 4
+// whose clusters all fit on the device at once with at least 1024 sites per
+// rank, else 1; a larger size when a replica fits shared memory only split.
+// `requested` = 0 picks automatically; 1, 2 or 4 forces that size (if the
+// specialised kernel applies and the parts fit shared memory).
+static void choose_cluster(Ctx &C, int requested) {
+    const size_t word = C.precision == CSMC_FP32 ? sizeof(float) : sizeof(double);
+    const int64_t limit = (int64_t)C.max_smem - 12 * 1024;
+    bool fast = true;
+    for (auto &S : C.sys) fast = fast && S->fast_ok;
+    auto fits = [&](int c, bool prefer) {
+        if (c == 1) {
+            for (auto &S : C.sys)
+                if (S->plan.Np > 65536 || 3 * S->plan.Np * (int64_t)word > limit) return false;
+            return true;
+        }
+        for (auto &S : C.sys) {
+            const int64_t per_rank = (S->plan.Np + c - 1) / c + 32 * (S->plan.n_colours + 1);
+            if (per_rank > 16384 || 3 * per_rank * (int64_t)word > limit) return false;
+            if (prefer && S->plan.N / c < 1024) return false;
+        }
+        return !prefer || (int64_t)C.n_items * c <= C.n_sms;
+    };
+    int best = 1;
+    if (requested > 0) {
+        require(requested == 1 || requested == 2 || requested == 4, CSMC_ERR_INVALID, "cluster size must be 1, 2 or 4");
+        require(requested == 1 || (fast && fits(requested, false)), CSMC_ERR_UNSUPPORTED,
+                "this cluster size needs lattices without cubic/quartic terms, one basis per colour class, and "
+                "parts that fit shared memory");
+        best = requested;
+    } else if (fast) {
+        int pick = 0;
+        for (int c : {1, 2, 4})
+            if (fits(c, true)) pick = c;
+        if (!pick) // no preferred size: the smallest one that fits
+            for (int c : {1, 2, 4})
+                if (fits(c, false)) {
+                    pick = c;
+                    break;
+                }
+        best = pick ? pick : 1;
+    }
+    C.cl = best;
+    for (auto &Sp : C.sys) {
+        System &S = *Sp;
+        if (best > 1) {
+            S.cl_layout = make_cluster_layout(S.plan, best);
+            S.q2c.upload(S.cl_layout.q2);
+            {
+                const ClusterLayout &L = S.cl_layout;
+                const int W = std::max(S.plan.W2, 1);
+                std::vector<uint4> all;
+                for (int k = 0; k < L.ranks; k++) {
+                    std::vector<uint16_t> part(L.q2.begin() + (size_t)k * W * L.Npl,
+                                               L.q2.begin() + (size_t)(k + 1) * W * L.Npl);
+                    const uint32_t sent = (uint32_t)((k << 14) | (L.Npl - 32));
+                    std::vector<uint4> pk = pack8(part, S.plan.W2, L.Npl, [&](int64_t) { return sent; });
+                    all.insert(all.end(), pk.begin(), pk.end());
+                }
+                S.q2v.upload(all);
+            }
+            S.resident_smem = 3 * S.cl_layout.Npl * word;
+            S.resident_ok = (int64_t)S.resident_smem <= limit && S.plan.n_colours <= CSMC_MAX_COLOURS;
+        } else {
+            S.cl_layout = ClusterLayout();
+            S.resident_smem = 3 * S.plan.Np * word;
+            S.resident_ok = S.plan.Np <= 65536 && (int64_t)S.resident_smem <= limit &&
+                            S.plan.n_colours <= CSMC_MAX_COLOURS;
+        }
+    }
+}
+
+// Resident descriptors of every lattice and the work list (largest replicas first).
+static void upload_resident(Ctx &C) {
+    std::vector<ResSys<float>> fr;
+    std::vector<ResSys<double>> dr;
+    std::vector<int2> items;
+    for (size_t k = 0; k < C.sys.size(); k++) {
+        System &S = *C.sys[k];
+        if (C.precision == CSMC_FP32) fr.push_back(make_res(S, S.fa));
+        else dr.push_back(make_res(S, S.da));
+        for (int r = 0; r < S.R; r++) items.push_back(make_int2((int)k, r));
+    }
+    std::stable_sort(items.begin(), items.end(),
+                     [&](int2 a, int2 b) { return C.sys[a.x]->plan.Np > C.sys[b.x]->plan.Np; });
+    if (C.precision == CSMC_FP32) C.fres.upload(fr);
+    else C.dres.upload(dr);
+    C.items.upload(items);
+    C.n_items = (int)items.size();
 }
 
 static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, int precision, uint64_t seed) {
@@ -387,23 +512,10 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.drift_bits = C->drift_bits.p;
     cs.error_flag = C->error_flag.p;
 
-    // resident descriptors and the work list (largest replicas first)
-    std::vector<ResSys<float>> fr;
-    std::vector<ResSys<double>> dr;
-    std::vector<int2> items;
-    for (size_t k = 0; k < C->sys.size(); k++) {
-        System &S = *C->sys[k];
-        if (precision == CSMC_FP32) fr.push_back(make_res(S, S.fa));
-        else dr.push_back(make_res(S, S.da));
-        for (int r = 0; r < S.R; r++) items.push_back(make_int2((int)k, r));
-    }
-    std::stable_sort(items.begin(), items.end(), [&](int2 a, int2 b) {
-        return C->sys[a.x]->plan.Np > C->sys[b.x]->plan.Np;
-    });
-    if (precision == CSMC_FP32) C->fres.upload(fr);
-    else C->dres.upload(dr);
-    C->items.upload(items);
-    C->n_items = (int)items.size();
+    C->n_items = 0;
+    for (auto &S : C->sys) C->n_items += S->R;
+    choose_cluster(*C, 0);
+    upload_resident(*C);
     CK(cudaDeviceSynchronize());
     return C.release();
 }
@@ -543,6 +655,18 @@ static void sweep_global(Ctx &C, int what, int kind, double T_override, bool per
         }
     }
     if (what == 1) C.msweep++;
+    C.nsweeps++;
+}
+
+static void renorm_all(Ctx &C, Launches &L);
+
+// Single precision: renormalise |s| = S when the context's total sweep count
+// passed a multiple of renorm_every since `before` (as the resident kernel
+// does after each iteration).
+static void renorm_check(Ctx &C, Launches &L, uint64_t before) {
+    if (C.precision != CSMC_FP32 || C.renorm_every <= 0) return;
+    const uint64_t e = (uint64_t)C.renorm_every;
+    if (C.nsweeps / e > before / e) renorm_all(C, L);
 }
 
 static void energy_all(Ctx &C, Launches &L) {
@@ -613,7 +737,7 @@ static int resident_block(Ctx &C, int hint) {
 // when all lattices allow it (with the widest coupling classes among them),
 // else the generic one.
 static ResidentSel resident_selection(const Ctx &C) {
-    ResidentSel sel{true, 0, 0, false, false};
+    ResidentSel sel{true, 0, 0, false, false, C.cl};
     for (auto &S : C.sys) {
         sel.fast = sel.fast && S->fast_ok;
         sel.bil = std::max(sel.bil, S->bil_class);
@@ -628,10 +752,12 @@ static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
     size_t smem = 0;
     for (auto &S : C.sys) smem = std::max(smem, S->resident_smem);
     const ResidentSel sel = resident_selection(C);
-    int per_sm = C.precision == CSMC_FP32 ? resident_max_blocks_per_sm<float>(block, smem, sel)
-                                          : resident_max_blocks_per_sm<double>(block, smem, sel);
-    require(per_sm >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on an SM with this shared memory size");
-    const int grid = std::min(C.n_items, C.n_sms * per_sm);
+    if (sel.fast) block = 1024; // the specialised kernel is built for 1024 threads
+    const int cap = C.precision == CSMC_FP32 ? resident_capacity<float>(block, smem, sel, C.n_sms)
+                                             : resident_capacity<double>(block, smem, sel, C.n_sms);
+    require(cap >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on the device with this shared memory size");
+    // CTAs (one per replica) or clusters (sel.cl CTAs per replica)
+    const int grid = std::min(C.n_items, cap) * std::max(sel.cl, 1);
     auto ev = C.next_kernel_events();
     CK(cudaMemsetAsync(C.work_ctr.p, 0, sizeof(int), C.st));
     CK(cudaEventRecord(ev.first, C.st));
@@ -735,10 +861,16 @@ static void run(Ctx &C, csmc_run_params *p) {
             rd.reset_sigma = 0;
             rd.n_slots = n_slots;
             rd.renorm_every = C.renorm_every;
+            rd.sweeps0 = C.nsweeps;
             rd.swap_enabled = s.swap_enabled ? 1 : 0;
             resident_launch(C, rd, block, L);
-            for (int64_t q = it; q <= to; q++)
-                if (s.is_metro(q)) C.msweep++;
+            for (int64_t q = it; q <= to; q++) {
+                if (s.is_metro(q)) {
+                    C.msweep++;
+                    C.nsweeps++;
+                }
+                if (s.or_rate != 0) C.nsweeps++;
+            }
             pending = false;
             if (ends_swap) {
                 swap_all(to);
@@ -756,15 +888,11 @@ static void run(Ctx &C, csmc_run_params *p) {
         }
     } else {
         const bool per_rep = path == CSMC_PATH_PER_REPLICA;
-        int since_renorm = 0;
         for (int64_t it = s.start; it < s.end; it++) {
-            if (s.or_rate != 0) {
-                sweep_global(C, 0, 0, 0.0, per_rep, L);
-                since_renorm++;
-            }
+            const uint64_t before = C.nsweeps;
+            if (s.or_rate != 0) sweep_global(C, 0, 0, 0.0, per_rep, L);
             if (s.is_metro(it)) {
                 sweep_global(C, 1, s.kind, 0.0, per_rep, L);
-                since_renorm++;
                 if (s.need_E(it)) energy_all(C, L);
                 if (s.is_swap(it)) swap_all(it);
             }
@@ -777,12 +905,8 @@ static void run(Ctx &C, csmc_run_params *p) {
                         L.n++;
                     }
             }
-            if (C.renorm_every > 0 && since_renorm >= C.renorm_every) {
-                renorm_all(C, L);
-                since_renorm = 0;
-            }
+            renorm_check(C, L, before);
         }
-        if (since_renorm > 0 && C.renorm_every > 0) renorm_all(C, L);
     }
     CK(cudaEventRecord(e1, C.st));
     sync_check(C);
@@ -846,30 +970,26 @@ static void anneal(Ctx &C, const double *temps, int n_temps, int64_t t_therm, in
                 rd.reset_sigma = 1;
                 rd.n_slots = n_slots;
                 rd.renorm_every = C.renorm_every;
+                rd.sweeps0 = C.nsweeps;
                 resident_launch(C, rd, resident_block(C, 0), L);
-                for (int64_t t = 1; t < t_therm; t++)
-                    if (t % dosweep == 0) C.msweep++;
+                for (int64_t t = 1; t < t_therm; t++) {
+                    if (t % dosweep == 0) {
+                        C.msweep++;
+                        C.nsweeps++;
+                    }
+                    if (or_rate != 0) C.nsweeps++;
+                }
             } else {
                 std::vector<double> sg(n_slots, sigma0);
                 CK(cudaMemcpyAsync(C.sigma_slot.p, sg.data(), n_slots * sizeof(double), cudaMemcpyHostToDevice, C.st));
                 CK(cudaStreamSynchronize(C.st));
                 const bool per_rep = path == CSMC_PATH_PER_REPLICA;
-                int since = 0;
                 for (int64_t t = 1; t < t_therm; t++) {
-                    if (or_rate != 0) {
-                        sweep_global(C, 0, 0, T, per_rep, L);
-                        since++;
-                    }
-                    if (t % dosweep == 0) {
-                        sweep_global(C, 1, kind, T, per_rep, L);
-                        since++;
-                    }
-                    if (C.renorm_every > 0 && since >= C.renorm_every) {
-                        renorm_all(C, L);
-                        since = 0;
-                    }
+                    const uint64_t before = C.nsweeps;
+                    if (or_rate != 0) sweep_global(C, 0, 0, T, per_rep, L);
+                    if (t % dosweep == 0) sweep_global(C, 1, kind, T, per_rep, L);
+                    renorm_check(C, L, before);
                 }
-                if (since > 0 && C.renorm_every > 0) renorm_all(C, L);
             }
         }
         CK(cudaEventRecord(e1, C.st));
@@ -1195,7 +1315,9 @@ int csmc_metropolis_sweep(void *c, int32_t kind, double *accepted) {
     Ctx &C = ctx_of(c);
     require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
     Launches L;
+    const uint64_t before = C.nsweeps;
     sweep_global(C, 1, kind, 0.0, false, L);
+    renorm_check(C, L, before);
     sync_check(C);
     if (accepted) {
         std::vector<double> a = download_f64(C.last_acc, C.n_chains);
@@ -1208,7 +1330,9 @@ int csmc_overrelax_sweep(void *c) {
     API_BEGIN
     Ctx &C = ctx_of(c);
     Launches L;
+    const uint64_t before = C.nsweeps;
     sweep_global(C, 0, 0, 0.0, false, L);
+    renorm_check(C, L, before);
     sync_check(C);
     API_END
 }
@@ -1218,7 +1342,11 @@ int csmc_deterministic_sweeps(void *c, int64_t n) {
     Ctx &C = ctx_of(c);
     require(n >= 0, CSMC_ERR_INVALID, "n_sweeps must be >= 0");
     Launches L;
-    for (int64_t k = 0; k < n; k++) sweep_global(C, 2, 0, 0.0, false, L);
+    for (int64_t k = 0; k < n; k++) {
+        const uint64_t before = C.nsweeps;
+        sweep_global(C, 2, 0, 0.0, false, L);
+        renorm_check(C, L, before);
+    }
     sync_check(C);
     API_END
 }
@@ -1281,6 +1409,23 @@ int csmc_anneal(void *c, const double *temps, int32_t n_temps, int64_t t_therm, 
                 double sigma0, int32_t path, double *accepted) {
     API_BEGIN
     anneal(ctx_of(c), temps, n_temps, t_therm, or_rate, kind, sigma0, path, accepted);
+    API_END
+}
+
+int csmc_set_cluster_size(void *c, int32_t ranks) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(ranks >= 0, CSMC_ERR_INVALID, "cluster size must be 0, 1, 2 or 4");
+    CK(cudaStreamSynchronize(C.st));
+    choose_cluster(C, ranks);
+    upload_resident(C);
+    API_END
+}
+
+int csmc_cluster_size(void *c, int32_t *ranks) {
+    API_BEGIN
+    require(ranks != nullptr, CSMC_ERR_INVALID, "ranks is NULL");
+    *ranks = ctx_of(c).cl;
     API_END
 }
 

@@ -189,16 +189,27 @@ __device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Co
 
 template <typename R> struct Math;
 template <> struct Math<float> {
-    static __device__ __forceinline__ void sincospi2(float u, float *s, float *c) { sincospif(2.0f * u, s, c); }
+    // sin and cos of 2*pi*u for u in [0,1): the hardware approximation on the
+    // angle shifted into [-pi, pi) (absolute error below 2^-21), then
+    // sin(a + pi) = -sin(a), cos(a + pi) = -cos(a)
+    static __device__ __forceinline__ void sincospi2(float u, float *s, float *c) {
+        float sa, ca;
+        __sincosf(6.28318530718f * (u - 0.5f), &sa, &ca);
+        *s = -sa;
+        *c = -ca;
+    }
     static __device__ __forceinline__ float sqrt_(float v) { return sqrtf(v); }
     static __device__ __forceinline__ float rsqrt_(float v) { return rsqrtf(v); }
     static __device__ __forceinline__ float exp_(float v) { return __expf(v); }
+    // a / b within 2 ulp for 2^-126 <= |b| <= 2^126 (the squared local field)
+    static __device__ __forceinline__ float div_(float a, float b) { return __fdividef(a, b); }
 };
 template <> struct Math<double> {
     static __device__ __forceinline__ void sincospi2(double u, double *s, double *c) { sincospi(2.0 * u, s, c); }
     static __device__ __forceinline__ double sqrt_(double v) { return sqrt(v); }
     static __device__ __forceinline__ double rsqrt_(double v) { return rsqrt(v); }
     static __device__ __forceinline__ double exp_(double v) { return exp(v); }
+    static __device__ __forceinline__ double div_(double a, double b) { return a / b; }
 };
 
 // Uniforms of one Metropolis proposal from the Philox stream keyed by the

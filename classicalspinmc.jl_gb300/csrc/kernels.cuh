@@ -49,7 +49,18 @@ template <typename R> struct ResSys {
     int64_t n_real;
     R S;
     uint32_t k0, k1;
+    // split over a cluster of `cl` CTAs (cl > 1): per rank and colour class,
+    // the local start, the site count and the device index of the first site;
+    // partners q2c[rank][W2][Npl] encoded (owner rank << 14) | owner-local index
+    int32_t cl, Npl;
+    int32_t loc_start[4][CSMC_MAX_COLOURS], loc_count[4][CSMC_MAX_COLOURS], src_start[4][CSMC_MAX_COLOURS];
+    const uint16_t *q2c;
+    // the bilinear partners of each site packed in one 16-byte word (up to 8
+    // 16-bit partners, sentinel-padded): p2v[i] for one CTA per replica,
+    // q2v[rank][i] for clusters; used by the specialised kernel
+    const uint4 *p2v, *q2v;
 };
+constexpr int RESIDENT_CLUSTER_MAX = 4;
 
 // Which resident kernel: the generic one (per-site pattern, cubic and
 // quartic terms) or the specialised one for lattices without cubic/quartic
@@ -60,6 +71,7 @@ struct ResidentSel {
     bool fast;
     int bil, ons;
     bool cub, qua;
+    int cl; // CTAs per replica (thread-block cluster size; 1 = no cluster)
 };
 constexpr int RESIDENT_WMAX = 8; // bilinear slots per site of the specialised kernel
 
@@ -78,6 +90,7 @@ struct RunDesc {
     int32_t reset_sigma;      // sigma <- sigma0 before the first sweep
     int32_t n_slots;
     int32_t renorm_every;     // single precision: renormalise every k sweeps
+    uint64_t sweeps0;         // the context's sweeps (all kinds) before this launch
     int32_t swap_enabled;
 };
 

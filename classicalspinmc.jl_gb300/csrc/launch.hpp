@@ -44,7 +44,8 @@ template <typename R>
 cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
                             const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem,
                             const ResidentSel &sel, cudaStream_t st);
-template <typename R> int resident_max_blocks_per_sm(int block, size_t smem, const ResidentSel &sel);
+// CTAs (cl = 1) or clusters (cl > 1) of the selected resident kernel that fit on the device at once
+template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms);
 
 // Reference-layout tables of one lattice for the replay kernel (exact.cu):
 // per reference site, N2/N3/N4 term entries with 0-based partners (-1 absent).

@@ -680,6 +680,57 @@ Plan make_plan(const csmc_lattice_desc *dd) {
     return P;
 }
 
+ClusterLayout make_cluster_layout(const Plan &P, int ranks) {
+    require(ranks >= 1 && ranks <= CLUSTER_MAX, CSMC_ERR_INVALID, "cluster size out of range");
+    ClusterLayout L;
+    L.ranks = ranks;
+    const int C = P.n_colours;
+    L.part.assign(C, 0);
+    L.loc_start.assign((size_t)ranks * C, 0);
+    L.loc_count.assign((size_t)ranks * C, 0);
+    L.src_start.assign((size_t)ranks * C, 0);
+    std::vector<int64_t> len(ranks, 0);
+    for (int c = 0; c < C; c++) {
+        const int64_t n = P.col_count[c];
+        L.part[c] = ((n + ranks - 1) / ranks + 31) / 32 * 32;
+        for (int k = 0; k < ranks; k++) {
+            const int64_t lo = std::min(n, k * L.part[c]), hi = std::min(n, (k + 1) * L.part[c]);
+            L.loc_start[k * C + c] = len[k];
+            L.loc_count[k * C + c] = hi - lo;
+            L.src_start[k * C + c] = P.col_start[c] + lo;
+            len[k] += (hi - lo + 31) / 32 * 32;
+        }
+    }
+    int64_t mx = 0;
+    for (int k = 0; k < ranks; k++) mx = std::max(mx, len[k]);
+    L.Npl = mx + 32; // sentinel block at local index mx
+    require(L.Npl <= 16384, CSMC_ERR_UNSUPPORTED, "a cluster rank would hold more than 16383 sites");
+    const int64_t sent_local = mx;
+    // device index -> (owner, local)
+    auto locate = [&](int64_t d, int reader) -> uint16_t {
+        if (d == P.sentinel || d < 0) return (uint16_t)((reader << 14) | sent_local);
+        int c = 0;
+        while (c + 1 < C && d >= P.col_start[c + 1]) c++;
+        const int64_t off = d - P.col_start[c];
+        const int k = (int)(off / L.part[c]);
+        const int64_t local = L.loc_start[k * C + c] + (off - k * L.part[c]);
+        return (uint16_t)((k << 14) | local);
+    };
+    const int W = std::max(P.W2, 1);
+    L.q2.assign((size_t)ranks * W * L.Npl, 0);
+    for (int k = 0; k < ranks; k++) {
+        for (int t = 0; t < W; t++)
+            for (int64_t i = 0; i < L.Npl; i++) L.q2[((size_t)k * W + t) * L.Npl + i] = (uint16_t)((k << 14) | sent_local);
+        for (int c = 0; c < C; c++)
+            for (int64_t j = 0; j < L.loc_count[k * C + c]; j++) {
+                const int64_t d = L.src_start[k * C + c] + j, i = L.loc_start[k * C + c] + j;
+                for (int t = 0; t < P.W2; t++)
+                    L.q2[((size_t)k * W + t) * L.Npl + i] = locate(P.p2[(size_t)t * P.Np + d], k);
+            }
+    }
+    return L;
+}
+
 void fill_info(const Plan &p, csmc_lattice_info *info) {
     std::memset(info, 0, sizeof(*info));
     info->n_sites = p.N;

@@ -81,6 +81,24 @@ struct Plan {
 // Build everything; throws csmc::Error.
 Plan make_plan(const csmc_lattice_desc *d);
 
+// Layout of one replica split over the CTAs of a thread-block cluster: rank
+// k holds part k of every colour class (parts of `part[c]` sites, a multiple
+// of 32, in device order), laid out class by class in its shared memory and
+// followed by a 32-site block of zeros (its sentinel).  Partners are encoded
+// (owner rank << 14) | owner-local index.
+constexpr int CLUSTER_MAX = 4;
+struct ClusterLayout {
+    int ranks = 1;
+    int64_t Npl = 0;                     // local length per rank (incl. sentinel block)
+    std::vector<int64_t> part;           // [colour] sites per part
+    std::vector<int64_t> loc_start;      // [rank][colour]
+    std::vector<int64_t> loc_count;      // [rank][colour]
+    std::vector<int64_t> src_start;      // [rank][colour] device index of the part's first site
+    std::vector<uint16_t> q2;            // [rank][W2][Npl]
+};
+// Throws csmc::Error if a rank would hold more than 16383 sites.
+ClusterLayout make_cluster_layout(const Plan &p, int ranks);
+
 void fill_info(const Plan &p, csmc_lattice_info *info);
 void export_tables(const Plan &p, int64_t *bs, double *bm, int64_t *cs, double *ct, int64_t *qs,
                    double *qt, double *field, double *onsite);

@@ -255,6 +255,15 @@ int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_therm
                 int32_t overrelaxation_rate, int32_t kind, double sigma0, int32_t path,
                 double *accepted);
 
+/* CTAs per replica of the resident kernel (a thread-block cluster that splits
+ * each replica's colour classes): 0 = automatic (the largest of 1, 2, 4 whose
+ * clusters all fit on the device with >= 1024 sites per CTA), or force 1, 2
+ * or 4.  Sizes above 1 need lattices without cubic/quartic terms and one
+ * basis per colour class (CSMC_ERR_UNSUPPORTED otherwise).  A tuning knob of
+ * this library; no counterpart in the reference. */
+int csmc_set_cluster_size(void *ctx, int32_t ranks);
+int csmc_cluster_size(void *ctx, int32_t *ranks);
+
 /* Spin-length renormalisation interval of the single-precision kernels, in
  * sweeps (0 = never).  Default 64. */
 int csmc_set_renormalize(void *ctx, int32_t every_sweeps);

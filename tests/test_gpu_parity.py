@@ -432,3 +432,61 @@ def test_fp32_energy_density_vs_fp64_oracle(m, orc):
     for r in range(2):
         s = mc.spins(r)
         assert abs(E[r] / lat.size - ol.total_energy(s) / lat.size) <= 1e-4
+
+
+def _cluster(mc, ranks=None):
+    import ctypes as C
+    if ranks is not None:
+        mc.ctx.call("csmc_set_cluster_size", ranks)
+    out = C.c_int32()
+    mc.ctx.call("csmc_cluster_size", C.byref(out))
+    return out.value
+
+
+@pytest.mark.parametrize("ranks", [2, 4])
+@pytest.mark.parametrize("name", ["square", "honeycomb", "sc", "sc24", "triangular_open", "asym_open", "selfloop"])
+def test_cluster_resident_single_sweeps_match_oracle(m, orc, name, ranks):
+    """The resident kernel split over a cluster of 2 or 4 CTAs (partners of
+    other ranks read through distributed shared memory) == the oracle, one
+    overrelaxation and one Metropolis sweep in colour order, FP64."""
+    seed = 23
+    lat, ol, mc = setup(m, orc, name, "fp64", seed=seed, T=0.6)
+    assert _cluster(mc, ranks) == ranks
+    _, order, _ = lat.colouring()
+    s = rand_spins(lat.size, 31)
+    mc.set_spins(s)
+    _run_once(m, mc, 1, 1, 1000, "resident")
+    ol.overrelax_order(s, order)
+    assert np.abs(mc.spins(0) - s).max() <= 1e-12
+    acc = _run_once(m, mc, 0, 1, 0, "resident")
+    acc_o, _ = ol.colour_sweep(s, 0.6, orc.UNIFORM, 60.0, order, seed, 0, 0, 53)
+    assert acc[0] == acc_o
+    assert np.abs(mc.spins(0) - s).max() <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["sc", "honeycomb", "triangular_open"])
+def test_cluster_sizes_give_the_same_chain(m, orc, name, precision):
+    """One CTA per replica and clusters of 2 and 4 CTAs run the same
+    arithmetic per site: a parallel-tempering window with exchanges, probes and
+    adaptive sigma gives the same spins, records and counters."""
+    res = []
+    for ranks in (1, 2, 4):
+        lat, ol, mc = setup(m, orc, name, precision, R=4, seed=9)
+        assert _cluster(mc, ranks) == ranks
+        mc.ctx.set_temperatures(np.array([0.2, 0.4, 0.8, 1.6]))
+        for r in range(4):
+            mc.set_spins(rand_spins(lat.size, 40 + r), r)
+        mc.path = "resident"
+        p = mc.parameters
+        p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 5, 35, 40, 10
+        p.probe_rate, p.swap_rate, p.overrelaxation_rate = 5, 5, 5
+        out = m.parallel_tempering(mc, alg=m.MetropolisAdaptive(), verbose=False)
+        res.append((np.stack([mc.spins(r) for r in range(4)]), out["energy"], out["magnetization"],
+                    mc.accepted.copy(), mc.exchanged.copy(), np.atleast_1d(mc.sigma)))
+    for other in res[1:]:
+        assert np.abs(res[0][0] - other[0]).max() <= 1e-12 * (1 if precision == "fp64" else 1e6)
+        assert np.abs(res[0][1] - other[1]).max() <= 1e-9 * lat.size
+        assert np.abs(res[0][2] - other[2]).max() <= 1e-9 * lat.size
+        assert np.array_equal(res[0][3], other[3]) and np.array_equal(res[0][4], other[4])
+        assert np.allclose(res[0][5], other[5], rtol=1e-12)
