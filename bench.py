@@ -271,6 +271,106 @@ def oracle_sample(target_s: float, threads: int):
                      "sample": f"{n} iterations (= {n // ITER_PER_STEP} steps) of the 64-replica L=24 workload"}
 
 
+# ------------------------------------------------------------------ other configurations
+# The remaining configurations of the path, each measured the same way
+# (device time of csmc_run / csmc_anneal through the C ABI, L2 flushed between
+# steps) beside the oracle on the host cores.  The driver's default line is the
+# 64-replica simple-cubic workload above; these are selected with --workload.
+
+def _triangular_batch(m, n=256, seed=4):
+    """256 independent triangular antiferromagnets: (L, T, h) per chain from a seeded generator."""
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice([12, 18, 24, 36, 48, 72], size=n)
+    Ts = np.exp(rng.uniform(math.log(0.05), math.log(1.0), size=n))
+    hs = rng.uniform(0.0, 3.0, size=n)
+    lats = [m.Lattice((int(L), int(L)), m.examples.triangular_afm(h=float(h)), 1.0, initialCondition="none")
+            for L, h in zip(Ls, hs)]
+    return lats, Ts, hs
+
+
+def other_workload(name, m):
+    """(lattices, replicas per lattice, temperatures per slot, precision, run kwargs, description)."""
+    E = m.examples
+    if name == "square_fp64":
+        lat = m.Lattice((32, 32), E.square_heisenberg(), 1.0, initialCondition="none")
+        return ([lat], [1], np.array([0.5]), "fp64", dict(or_rate=10, swap_rate=0, probe_rate=10, iters=100),
+                "square Heisenberg L=32 (1024 sites), h=(0,0,0.1), T=0.5, FP64, 100 iterations per step")
+    if name == "honeycomb_fp32":
+        lat = m.Lattice((48, 48), E.honeycomb_kitaev(K=-1.0, J=0.1, G=0.05), 1.0, initialCondition="none")
+        return ([lat], [1], np.array([1.0]), "fp32", dict(or_rate=10, swap_rate=0, probe_rate=0, iters=1000),
+                "honeycomb K-J-Gamma L=48 (4608 sites), one annealing temperature of 1000 iterations per step, FP32")
+    if name == "triangular_batch_fp32":
+        lats, Ts, _ = _triangular_batch(m)
+        return (lats, [1] * len(lats), Ts, "fp32", dict(or_rate=5, swap_rate=0, probe_rate=10, iters=10),
+                f"256 triangular AFM chains, L in {{12..72}} ({sum(l.size for l in lats)} sites), FP32")
+    if name in ("pyrochlore_fp32", "pyrochlore_large_fp32"):
+        shape = (16, 16, 16) if name == "pyrochlore_fp32" else (32, 32, 16)
+        lat = m.Lattice(shape, E.pyrochlore_ckq(), 1.0, initialCondition="none")
+        Ts = np.exp(np.linspace(math.log(0.05), math.log(1.5), 32))
+        return ([lat], [32], Ts, "fp32", dict(or_rate=5, swap_rate=10, probe_rate=10, iters=10),
+                f"pyrochlore J1 + cubic + quartic, shape {shape} ({lat.size} sites), 32 PT replicas, FP32")
+    raise SystemExit(f"unknown workload {name}")
+
+
+def bench_other(args):
+    import torch
+    m = G.load()
+    from importlib import import_module
+    L = import_module(m.__name__ + "._lib")
+    torch.cuda.set_device(0)
+    lats, reps, Ts, prec, kw, desc = other_workload(args.workload, m)
+    ctx = m.monte_carlo.Context(lats, reps, precision=prec, seed=SEED)
+    ctx.set_temperatures(Ts)
+    ctx.call("csmc_random_spins", C.c_uint64(SEED))
+    sites = sum(l.size * r for l, r in zip(lats, reps))
+    iters = kw["iters"]
+    anneal = args.workload == "honeycomb_fp32"
+    if anneal:
+        upd = sites * ((iters - 1) + (iters - 1) // kw["or_rate"])
+    else:
+        upd = sites * (iters + iters // kw["or_rate"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    it = [1]
+
+    def step():
+        if anneal:
+            temps = np.array([1.0])
+            ctx.call("csmc_anneal", temps.ctypes.data_as(C.POINTER(C.c_double)), 1, C.c_int64(iters),
+                     kw["or_rate"], L.METROPOLIS, C.c_double(60.0), L.PATH_AUTO, None)
+        else:
+            rp = L.RunParams()
+            rp.sweep_start, rp.n_sweeps, rp.t_thermalization = it[0], iters, 0
+            rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = kw["or_rate"], kw["swap_rate"], kw["probe_rate"]
+            rp.kind, rp.path = L.METROPOLIS, L.PATH_AUTO
+            ctx.call("csmc_run", C.byref(rp))
+            it[0] += iters
+        return stats(ctx)
+
+    for _ in range(args.warmup):
+        step()
+    t_dev = 0.0
+    launches = 0
+    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms, n, _, _ = step()
+            t_dev += ms / 1e3
+            launches += n
+    value = upd * args.steps / t_dev
+    cl = C.c_int32()
+    ctx.call("csmc_cluster_size", C.byref(cl))
+    line = {"metric": "site updates/s (Metropolis+OR)", "value": value, "unit": "site updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "site_updates_per_step": upd,
+                       "ctas_per_replica": cl.value, "l2": "flushed between steps (256 MB write)"},
+            "clocks": clk.summary(), "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -282,7 +382,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: library default; 1, 2 or 4)")
+    ap.add_argument("--workload", default="sc_pt",
+                    choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
+                             "pyrochlore_large_fp32"],
+                    help="sc_pt (default): the 64-replica simple-cubic line; the others measure the remaining "
+                         "configurations (device throughput only)")
     args = ap.parse_args()
+    if args.workload != "sc_pt":
+        bench_other(args)
+        return
     global RESIDENT_BLOCK
     RESIDENT_BLOCK = args.block
     rank = int(os.environ.get("RANK", "0"))

@@ -72,6 +72,7 @@ struct System {
     // the single basis of each colour class
     bool fast_ok = false;
     int bil_class = 1, ons_class = 2;
+    bool pv_stage = false; // partner words staged in shared memory beside the spins
     std::vector<int32_t> col_pattern;
     // split over a thread-block cluster (context-wide cluster size > 1)
     ClusterLayout cl_layout;
@@ -102,6 +103,7 @@ struct Ctx {
     DevBuf<ResSys<float>> fres;
     DevBuf<ResSys<double>> dres;
     DevBuf<int2> items;
+    DevBuf<int2> lattices; // per lattice {first slot, replicas} (exchange kernel)
     int n_items = 0;
     int cl = 1; // CTAs per replica of the resident kernel
     uint32_t msweep = 0;   // Metropolis sweeps so far (the Philox counter)
@@ -115,13 +117,33 @@ struct Ctx {
     double last_kernel_ms = 0.0;
     int64_t last_kernel_launches = 0;
     ChainState cs{};
+    // pinned host staging for the results of a run (error flag, probe
+    // records, counters): copied back together, read after one synchronisation
+    int *h_flag = nullptr;
+    double *h_box = nullptr;
+    size_t h_box_n = 0;
+    cudaEvent_t run_e0 = nullptr, run_e1 = nullptr;
 
     ~Ctx() {
         for (auto &e : kev) {
             cudaEventDestroy(e.first);
             cudaEventDestroy(e.second);
         }
+        if (run_e0) cudaEventDestroy(run_e0);
+        if (run_e1) cudaEventDestroy(run_e1);
+        if (h_flag) cudaFreeHost(h_flag);
+        if (h_box) cudaFreeHost(h_box);
         if (st) cudaStreamDestroy(st);
+    }
+    double *host_box(size_t n) {
+        if (n > h_box_n) {
+            if (h_box) cudaFreeHost(h_box);
+            h_box = nullptr;
+            h_box_n = 0;
+            CK(cudaHostAlloc((void **)&h_box, n * sizeof(double), cudaHostAllocDefault));
+            h_box_n = n;
+        }
+        return h_box;
     }
     std::pair<cudaEvent_t, cudaEvent_t> next_kernel_events() {
         if (kev_used == kev.size()) {
@@ -266,8 +288,8 @@ static void upload_system(Ctx &C, System &S) {
         a.cub = S.cub;
         a.qua = S.qua;
     };
-    const size_t nsp = (size_t)S.R * 3 * Np;
     if (C.precision == CSMC_FP32) {
+        const size_t nsp = (size_t)S.R * 4 * Np; // one float4 per site
         S.fmats.upload(to_f(P.mats));
         S.fcubs.upload(to_f(P.cubs));
         S.fquas.upload(to_f(P.quas));
@@ -286,8 +308,8 @@ static void upload_system(Ctx &C, System &S) {
         S.fa.cf.E2 = S.fE2.p;
         S.fa.cf.Js = S.fJs.p;
         S.fa.S = (float)P.desc.S;
-        S.resident_smem = 3 * Np * sizeof(float);
     } else {
+        const size_t nsp = (size_t)S.R * 3 * Np; // x | y | z blocks
         S.dmats.upload(P.mats);
         S.dcubs.upload(P.cubs);
         S.dquas.upload(P.quas);
@@ -306,12 +328,7 @@ static void upload_system(Ctx &C, System &S) {
         S.da.cf.E2 = S.dE2.p;
         S.da.cf.Js = S.dJs.p;
         S.da.S = P.desc.S;
-        S.resident_smem = 3 * Np * sizeof(double);
     }
-    // dynamic shared memory holds the replica; keep 12 KB for the kernel's
-    // static shared memory (descriptor, reduction scratch, staged couplings)
-    S.resident_ok = P.Np <= 65536 && (int64_t)S.resident_smem <= (int64_t)C.max_smem - 12 * 1024 &&
-                    P.n_colours <= CSMC_MAX_COLOURS;
 }
 
 template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R> &a) {
@@ -343,6 +360,7 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     r.q2c = S.q2c.p;
     r.p2v = S.p2v.p;
     r.q2v = S.q2v.p;
+    r.pv_stage = S.pv_stage ? 1 : 0;
     if (L.ranks > 1)
         for (int k = 0; k < L.ranks; k++)
             for (int c = 0; c < S.plan.n_colours; c++) {
@@ -353,25 +371,30 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     return r;
 }
 
+// Bytes of shared memory for the spins of n sites (float4 or three doubles per site).
+static int64_t spin_bytes(const Ctx &C, int64_t n) { return C.precision == CSMC_FP32 ? 16 * n : 24 * n; }
+// Dynamic shared memory a resident CTA may use: the opt-in maximum less a
+// reserve for the kernel's static shared memory (at most about 6 KB).
+static int64_t dynamic_smem_limit(const Ctx &C) { return (int64_t)C.max_smem - 8 * 1024; }
+
 // Cluster size of the resident kernel for a context: the largest of 2 and 4
 // whose clusters all fit on the device at once with at least 1024 sites per
 // rank, else 1; a larger size when a replica fits shared memory only split.
 // `requested` = 0 picks automatically; 1, 2 or 4 forces that size (if the
 // specialised kernel applies and the parts fit shared memory).
 static void choose_cluster(Ctx &C, int requested) {
-    const size_t word = C.precision == CSMC_FP32 ? sizeof(float) : sizeof(double);
-    const int64_t limit = (int64_t)C.max_smem - 12 * 1024;
+    const int64_t limit = dynamic_smem_limit(C);
     bool fast = true;
     for (auto &S : C.sys) fast = fast && S->fast_ok;
     auto fits = [&](int c, bool prefer) {
         if (c == 1) {
             for (auto &S : C.sys)
-                if (S->plan.Np > 65536 || 3 * S->plan.Np * (int64_t)word > limit) return false;
+                if (S->plan.Np > 65536 || spin_bytes(C, S->plan.Np) > limit) return false;
             return true;
         }
         for (auto &S : C.sys) {
             const int64_t per_rank = (S->plan.Np + c - 1) / c + 32 * (S->plan.n_colours + 1);
-            if (per_rank > 16384 || 3 * per_rank * (int64_t)word > limit) return false;
+            if (per_rank > 16384 || spin_bytes(C, per_rank) > limit) return false;
             if (prefer && S->plan.N / c < 1024) return false;
         }
         return !prefer || (int64_t)C.n_items * c <= C.n_sms;
@@ -414,19 +437,38 @@ static void choose_cluster(Ctx &C, int requested) {
                 }
                 S.q2v.upload(all);
             }
-            S.resident_smem = 3 * S.cl_layout.Npl * word;
+            S.resident_smem = (size_t)spin_bytes(C, S.cl_layout.Npl);
             S.resident_ok = (int64_t)S.resident_smem <= limit && S.plan.n_colours <= CSMC_MAX_COLOURS;
         } else {
             S.cl_layout = ClusterLayout();
-            S.resident_smem = 3 * S.plan.Np * word;
+            S.resident_smem = (size_t)spin_bytes(C, S.plan.Np);
             S.resident_ok = S.plan.Np <= 65536 && (int64_t)S.resident_smem <= limit &&
                             S.plan.n_colours <= CSMC_MAX_COLOURS;
         }
     }
 }
 
-// Resident descriptors of every lattice and the work list (largest replicas first).
+static ResidentSel resident_selection(const Ctx &C);
+
+// Resident descriptors of every lattice and the work list (largest replicas
+// first).  The specialised kernel also stages each CTA's packed partner
+// words in shared memory when they fit beside the spins of every lattice.
 static void upload_resident(Ctx &C) {
+    const ResidentSel sel = resident_selection(C);
+    const int stat = !sel.fast ? -1
+                     : C.precision == CSMC_FP32 ? resident_static_smem<float>(sel)
+                                                : resident_static_smem<double>(sel);
+    bool stage = sel.fast && stat >= 0;
+    for (auto &S : C.sys) {
+        const int64_t nl = C.cl > 1 ? S->cl_layout.Npl : S->plan.Np;
+        const int64_t spins = (spin_bytes(C, nl) + 15) / 16 * 16;
+        stage = stage && spins + 16 * nl + stat <= (int64_t)C.max_smem;
+    }
+    for (auto &S : C.sys) {
+        const int64_t nl = C.cl > 1 ? S->cl_layout.Npl : S->plan.Np;
+        S->pv_stage = stage;
+        S->resident_smem = (size_t)(stage ? (spin_bytes(C, nl) + 15) / 16 * 16 + 16 * nl : spin_bytes(C, nl));
+    }
     std::vector<ResSys<float>> fr;
     std::vector<ResSys<double>> dr;
     std::vector<int2> items;
@@ -512,6 +554,13 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.drift_bits = C->drift_bits.p;
     cs.error_flag = C->error_flag.p;
 
+    std::vector<int2> lat;
+    for (auto &S : C->sys) lat.push_back(make_int2(S->base, S->R));
+    C->lattices.upload(lat);
+    CK(cudaHostAlloc((void **)&C->h_flag, sizeof(int), cudaHostAllocDefault));
+    *C->h_flag = 0;
+    CK(cudaEventCreate(&C->run_e0));
+    CK(cudaEventCreate(&C->run_e1));
     C->n_items = 0;
     for (auto &S : C->sys) C->n_items += S->R;
     choose_cluster(*C, 0);
@@ -522,16 +571,24 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
 
 // ------------------------------------------------------------ helpers
 
+// Enqueue the copy of the device error flag; after the stream is
+// synchronised, raise_flag() turns a set flag into CSMC_ERR_TIMEOUT.
+static void queue_flag(Ctx &C) {
+    CK(cudaMemcpyAsync(C.h_flag, C.error_flag.p, sizeof(int), cudaMemcpyDeviceToHost, C.st));
+}
+static void raise_flag(Ctx &C) {
+    if (*C.h_flag) {
+        *C.h_flag = 0;
+        CK(cudaMemset(C.error_flag.p, 0, sizeof(int)));
+        throw Error(CSMC_ERR_TIMEOUT, "a bounded device wait gave up (TMA staging or a cluster barrier did not complete)");
+    }
+}
+
 static void sync_check(Ctx &C) {
+    queue_flag(C);
     CK(cudaStreamSynchronize(C.st));
     CK(cudaGetLastError());
-    int flag = 0;
-    CK(cudaMemcpy(&flag, C.error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flag) {
-        int z = 0;
-        CK(cudaMemcpy(C.error_flag.p, &z, sizeof(int), cudaMemcpyHostToDevice));
-        throw Error(CSMC_ERR_TIMEOUT, "a bounded device wait gave up (TMA staging did not complete)");
-    }
+    raise_flag(C);
 }
 
 static std::vector<int32_t> download_i32(const DevBuf<int32_t> &b) {
@@ -551,69 +608,66 @@ template <class F> static void with_args(Ctx &C, System &S, F &&f) {
     else f(S.da);
 }
 
+// A host buffer the device can address directly (pinned or registered host
+// memory, mapped into the unified address space), or nullptr.
+static const double *device_view(const void *host) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    return static_cast<const double *>(at.devicePointer);
+}
+
+// Slots [first, first+n) of one lattice from / to the FP64 reference layout:
+// one conversion launch, reading or writing pinned host memory directly when
+// the caller's buffer is pinned, else through the device staging buffer.
+// Returns after the host buffer has been read (set) or written (get).
+static void set_spins_range(Ctx &C, System &S, int first, int n, const double *host) {
+    if (n <= 0) return;
+    const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
+    const double *src = device_view(host);
+    if (!src) {
+        CK(cudaMemcpyAsync(C.stage.p, host, bytes, cudaMemcpyHostToDevice, C.st));
+        src = C.stage.p;
+    }
+    with_args(C, S, [&](auto &a) { launch_scatter(a, C.chain_of.p, first, n, src, C.st); });
+    CK(cudaStreamSynchronize(C.st));
+}
+
+static void get_spins_range(Ctx &C, System &S, int first, int n, double *host) {
+    if (n <= 0) return;
+    const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
+    double *dst = const_cast<double *>(device_view(host));
+    const bool direct = dst != nullptr;
+    if (!direct) dst = C.stage.p;
+    with_args(C, S, [&](auto &a) { launch_gather(a, C.chain_of.p, first, n, dst, C.st); });
+    if (!direct) CK(cudaMemcpyAsync(host, C.stage.p, bytes, cudaMemcpyDeviceToHost, C.st));
+    CK(cudaStreamSynchronize(C.st));
+}
+
 static void set_spins_slot(Ctx &C, int slot, const double *host) {
-    const int k = C.sys_of_slot(slot);
-    System &S = *C.sys[k];
-    const int chain = download_i32(C.chain_of)[slot];
-    const int r = chain - S.base;
-    CK(cudaMemcpyAsync(C.stage.p, host, (size_t)S.plan.N * 3 * sizeof(double), cudaMemcpyHostToDevice, C.st));
-    with_args(C, S, [&](auto &a) { launch_scatter(a, r, 1, C.stage.p, C.st); });
+    set_spins_range(C, *C.sys[C.sys_of_slot(slot)], slot, 1, host);
 }
 
 static void get_spins_slot(Ctx &C, int slot, double *host) {
-    const int k = C.sys_of_slot(slot);
-    System &S = *C.sys[k];
-    const int chain = download_i32(C.chain_of)[slot];
-    const int r = chain - S.base;
-    with_args(C, S, [&](auto &a) { launch_gather(a, r, 1, C.stage.p, C.st); });
-    CK(cudaMemcpyAsync(host, C.stage.p, (size_t)S.plan.N * 3 * sizeof(double), cudaMemcpyDeviceToHost, C.st));
-}
-
-static bool identity_perm(const std::vector<int32_t> &chain_of, const System &S) {
-    for (int r = 0; r < S.R; r++)
-        if (chain_of[S.base + r] != S.base + r) return false;
-    return true;
+    get_spins_range(C, *C.sys[C.sys_of_slot(slot)], slot, 1, host);
 }
 
 static void set_spins_all(Ctx &C, const double *host) {
-    const std::vector<int32_t> chain_of = download_i32(C.chain_of);
     size_t off = 0;
     for (auto &Sp : C.sys) {
-        System &S = *Sp;
-        const size_t per = (size_t)S.plan.N * 3;
-        if (identity_perm(chain_of, S)) {
-            CK(cudaMemcpyAsync(C.stage.p, host + off, per * S.R * sizeof(double), cudaMemcpyHostToDevice, C.st));
-            with_args(C, S, [&](auto &a) { launch_scatter(a, 0, S.R, C.stage.p, C.st); });
-        } else {
-            for (int r = 0; r < S.R; r++) {
-                CK(cudaMemcpyAsync(C.stage.p, host + off + r * per, per * sizeof(double), cudaMemcpyHostToDevice,
-                                   C.st));
-                const int cr = chain_of[S.base + r] - S.base;
-                with_args(C, S, [&](auto &a) { launch_scatter(a, cr, 1, C.stage.p, C.st); });
-            }
-        }
-        off += per * S.R;
+        set_spins_range(C, *Sp, Sp->base, Sp->R, host + off);
+        off += (size_t)Sp->plan.N * 3 * Sp->R;
     }
 }
 
 static void get_spins_all(Ctx &C, double *host) {
-    const std::vector<int32_t> chain_of = download_i32(C.chain_of);
     size_t off = 0;
     for (auto &Sp : C.sys) {
-        System &S = *Sp;
-        const size_t per = (size_t)S.plan.N * 3;
-        if (identity_perm(chain_of, S)) {
-            with_args(C, S, [&](auto &a) { launch_gather(a, 0, S.R, C.stage.p, C.st); });
-            CK(cudaMemcpyAsync(host + off, C.stage.p, per * S.R * sizeof(double), cudaMemcpyDeviceToHost, C.st));
-        } else {
-            for (int r = 0; r < S.R; r++) {
-                const int cr = chain_of[S.base + r] - S.base;
-                with_args(C, S, [&](auto &a) { launch_gather(a, cr, 1, C.stage.p, C.st); });
-                CK(cudaMemcpyAsync(host + off + r * per, C.stage.p, per * sizeof(double), cudaMemcpyDeviceToHost,
-                                   C.st));
-            }
-        }
-        off += per * S.R;
+        get_spins_range(C, *Sp, Sp->base, Sp->R, host + off);
+        off += (size_t)Sp->plan.N * 3 * Sp->R;
     }
 }
 
@@ -724,24 +778,44 @@ static int choose_path(Ctx &C, int requested) {
     return all ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
 }
 
-static ResidentSel resident_selection(const Ctx &C);
-
-// 512 or 1024 threads per CTA; by default 1024 for the specialised kernel
-// (fits 64 registers) and 512 for the generic one (needs more registers).
+// Threads per CTA of the resident kernel.  `hint` (a multiple of 32) forces a
+// size, capped at the kernel's maximum (1024 for the specialised kernel with
+// scalar couplings and at most diagonal onsite terms, else 512).  Otherwise
+// the specialised kernel gets the smallest multiple of 32 that gives every
+// thread the same number of sites of the largest colour-class part between
+// two barriers, and the generic kernel its maximum.
 static int resident_block(Ctx &C, int hint) {
-    if (hint == 512 || hint == 1024) return hint;
-    return resident_selection(C).fast ? 1024 : 512;
+    const ResidentSel sel = resident_selection(C);
+    const int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
+    if (hint > 0) {
+        require(hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
+        return std::min(hint, mx);
+    }
+    if (!sel.fast) return mx;
+    int64_t n = 32;
+    for (auto &S : C.sys) {
+        const Plan &P = S->plan;
+        for (int col = 0; col < P.n_colours; col++) {
+            if (C.cl > 1)
+                for (int k = 0; k < C.cl; k++) n = std::max(n, S->cl_layout.loc_count[(size_t)k * P.n_colours + col]);
+            else
+                n = std::max(n, P.col_count[col]);
+        }
+    }
+    const int64_t iters = (n + mx - 1) / mx;
+    return (int)std::min<int64_t>(mx, (n + 32 * iters - 1) / (32 * iters) * 32);
 }
 
 // The resident kernel for every lattice of the context: the specialised one
 // when all lattices allow it (with the widest coupling classes among them),
 // else the generic one.
 static ResidentSel resident_selection(const Ctx &C) {
-    ResidentSel sel{true, 0, 0, false, false, C.cl};
+    ResidentSel sel{true, 0, 0, 4, false, false, C.cl};
     for (auto &S : C.sys) {
         sel.fast = sel.fast && S->fast_ok;
         sel.bil = std::max(sel.bil, S->bil_class);
         sel.ons = std::max(sel.ons, S->ons_class);
+        sel.width = std::max(sel.width, S->plan.W2 <= 4 ? 4 : S->plan.W2 <= 6 ? 6 : 8);
         sel.cub = sel.cub || S->cub;
         sel.qua = sel.qua || S->qua;
     }
@@ -752,7 +826,6 @@ static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
     size_t smem = 0;
     for (auto &S : C.sys) smem = std::max(smem, S->resident_smem);
     const ResidentSel sel = resident_selection(C);
-    if (sel.fast) block = 1024; // the specialised kernel is built for 1024 threads
     const int cap = C.precision == CSMC_FP32 ? resident_capacity<float>(block, smem, sel, C.n_sms)
                                              : resident_capacity<double>(block, smem, sel, C.n_sms);
     require(cap >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on the device with this shared memory size");
@@ -809,20 +882,22 @@ static void run(Ctx &C, csmc_run_params *p) {
     const int path = choose_path(C, p->path);
     C.reset_kernel_time();
     Launches L;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    cudaEvent_t e0 = C.run_e0, e1 = C.run_e1;
     CK(cudaEventRecord(e0, C.st));
 
-    auto swap_all = [&](int64_t it) {
-        for (size_t k = 0; k < C.sys.size(); k++) {
-            System &S = *C.sys[k];
-            if (S.R < 2) continue;
-            launch_swap(C.cs, S.base, S.R, it, s.swap_rate, (uint32_t)k, C.k0, C.k1, C.st);
-            L.n++;
-        }
+    // the exchange of iteration `it` (every lattice, one launch), followed by
+    // probe record kq (kq < 0: none)
+    auto exchange = [&](int64_t it, bool do_swap, int64_t kq) {
+        launch_exchange(C.cs, C.lattices.p, (int)C.sys.size(), it, s.swap_rate, C.k0, C.k1, do_swap, recE, recM, kq,
+                        n_slots, C.st);
+        L.n++;
     };
-    auto probe_index = [&](int64_t q) { return (q - s.probe_first) / s.probe_rate; };
+    // probe record index of iteration q, or -1 (no probe, or beyond the capacity)
+    auto record_index = [&](int64_t q) -> int64_t {
+        if (!s.is_probe(q)) return -1;
+        const int64_t kq = (q - s.probe_first) / s.probe_rate;
+        return kq < s.cap ? kq : -1;
+    };
 
     if (path == CSMC_PATH_RESIDENT) {
         const int block = resident_block(C, p->resident_block);
@@ -830,7 +905,6 @@ static void run(Ctx &C, csmc_run_params *p) {
         // `chunk` iterations per launch
         const int64_t chunk = 256;
         int64_t it = s.start;
-        bool pending = false;
         while (it < s.end) {
             int64_t to = std::min(s.end, it + chunk) - 1;
             bool ends_swap = false;
@@ -857,7 +931,6 @@ static void run(Ctx &C, csmc_run_params *p) {
             rd.swap_rate = s.swap_rate;
             rd.probe_rate = s.probe_rate;
             rd.kind = s.kind;
-            rd.pending_probe = pending ? 1 : 0;
             rd.reset_sigma = 0;
             rd.n_slots = n_slots;
             rd.renorm_every = C.renorm_every;
@@ -871,20 +944,10 @@ static void run(Ctx &C, csmc_run_params *p) {
                 }
                 if (s.or_rate != 0) C.nsweeps++;
             }
-            pending = false;
-            if (ends_swap) {
-                swap_all(to);
-                pending = s.is_probe(to);
-            }
+            // the kernel left |M| of an exchange iteration's probe in M_chain;
+            // the record follows the exchange
+            if (ends_swap) exchange(to, true, record_index(to));
             it = to + 1;
-        }
-        if (pending) { // the last exchange iteration was also a probe
-            magnet_all(C, L);
-            for (auto &S : C.sys) {
-                const int64_t kq = probe_index(s.end - 1);
-                if (kq < s.cap) launch_probe_record(C.cs, S->base, S->R, recE, recM, kq, n_slots, C.st);
-                L.n++;
-            }
         }
     } else {
         const bool per_rep = path == CSMC_PATH_PER_REPLICA;
@@ -894,44 +957,43 @@ static void run(Ctx &C, csmc_run_params *p) {
             if (s.is_metro(it)) {
                 sweep_global(C, 1, s.kind, 0.0, per_rep, L);
                 if (s.need_E(it)) energy_all(C, L);
-                if (s.is_swap(it)) swap_all(it);
             }
-            if (s.is_probe(it)) {
-                magnet_all(C, L);
-                const int64_t kq = probe_index(it);
-                if (kq < s.cap)
-                    for (auto &S : C.sys) {
-                        launch_probe_record(C.cs, S->base, S->R, recE, recM, kq, n_slots, C.st);
-                        L.n++;
-                    }
-            }
+            // |M| is per replica, unchanged by the exchange; the probe records
+            // by slot after it (monte_carlo.jl:308-349 then :368-370)
+            if (s.is_probe(it)) magnet_all(C, L);
+            const int64_t kq = record_index(it);
+            if (s.is_swap(it) || kq >= 0) exchange(it, s.is_swap(it), kq);
             renorm_check(C, L, before);
         }
     }
     CK(cudaEventRecord(e1, C.st));
-    sync_check(C);
+    // results into pinned staging, then one synchronisation
+    const size_t nrec = (size_t)s.cap * n_slots;
+    double *hb = C.host_box(2 * nrec + 2 * (size_t)n_slots);
+    double *h_E = hb, *h_M = hb + nrec, *h_acc = hb + 2 * nrec, *h_exch = h_acc + n_slots;
+    queue_flag(C);
+    if (nrec && p->probe_energy)
+        CK(cudaMemcpyAsync(h_E, C.rec_E.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    if (nrec && p->probe_magnetization)
+        CK(cudaMemcpyAsync(h_M, C.rec_M.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    if (p->accepted) CK(cudaMemcpyAsync(h_acc, C.acc_slot.p, n_slots * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    if (p->exchanged)
+        CK(cudaMemcpyAsync(h_exch, C.exch_slot.p, n_slots * sizeof(double), cudaMemcpyDeviceToHost, C.st));
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaGetLastError());
+    raise_flag(C);
     C.collect_kernel_time();
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     C.last_ms = ms;
     C.last_launches = L.n;
 
-    if (s.cap > 0) {
-        const size_t n = (size_t)s.cap * n_slots;
-        if (p->probe_energy) CK(cudaMemcpy(p->probe_energy, C.rec_E.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-        if (p->probe_magnetization)
-            CK(cudaMemcpy(p->probe_magnetization, C.rec_M.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-    }
-    if (p->accepted) {
-        std::vector<double> a = download_f64(C.acc_slot, n_slots);
-        for (int q = 0; q < n_slots; q++) p->accepted[q] += a[q];
-    }
-    if (p->exchanged) {
-        std::vector<double> a = download_f64(C.exch_slot, n_slots);
-        for (int q = 0; q < n_slots; q++) p->exchanged[q] += a[q];
-    }
+    if (nrec && p->probe_energy) std::memcpy(p->probe_energy, h_E, nrec * sizeof(double));
+    if (nrec && p->probe_magnetization) std::memcpy(p->probe_magnetization, h_M, nrec * sizeof(double));
+    if (p->accepted)
+        for (int q = 0; q < n_slots; q++) p->accepted[q] += h_acc[q];
+    if (p->exchanged)
+        for (int q = 0; q < n_slots; q++) p->exchanged[q] += h_exch[q];
     p->n_probes_out = s.cap;
 }
 
@@ -1134,7 +1196,7 @@ int csmc_set_spins(void *c, int32_t slot, const double *spins) {
     Ctx &C = ctx_of(c);
     require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
     set_spins_slot(C, slot, spins);
-    sync_check(C);
+    CK(cudaGetLastError());
     API_END
 }
 
@@ -1143,7 +1205,7 @@ int csmc_get_spins(void *c, int32_t slot, double *spins) {
     Ctx &C = ctx_of(c);
     require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
     get_spins_slot(C, slot, spins);
-    sync_check(C);
+    CK(cudaGetLastError());
     API_END
 }
 
@@ -1152,7 +1214,7 @@ int csmc_set_spins_all(void *c, const double *spins) {
     Ctx &C = ctx_of(c);
     require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
     set_spins_all(C, spins);
-    sync_check(C);
+    CK(cudaGetLastError());
     API_END
 }
 
@@ -1161,7 +1223,7 @@ int csmc_get_spins_all(void *c, double *spins) {
     Ctx &C = ctx_of(c);
     require(spins != nullptr, CSMC_ERR_INVALID, "spins is NULL");
     get_spins_all(C, spins);
-    sync_check(C);
+    CK(cudaGetLastError());
     API_END
 }
 

@@ -71,13 +71,51 @@ template <typename R> struct V3 {
     R x, y, z;
 };
 
+// The spins of one replica in device memory.  Single precision: one float4
+// (x, y, z, 0) per device site, so a site is a single 16-byte load and a
+// replica one contiguous block of 16 * Np bytes.  Double precision: three
+// blocks x[Np] | y[Np] | z[Np].  get/set take the device site index.
+template <typename R> struct Spins;
+template <> struct Spins<float> {
+    float4 *p;
+    static constexpr int kWords = 4; // floats per site
+    __device__ __forceinline__ V3<float> get(int64_t j) const {
+        const float4 v = p[j];
+        return {v.x, v.y, v.z};
+    }
+    __device__ __forceinline__ void set(int64_t j, V3<float> s) const { p[j] = make_float4(s.x, s.y, s.z, 0.f); }
+    // component k (0, 1, 2) of site j
+    __device__ __forceinline__ float get1(int64_t j, int k) const { return reinterpret_cast<const float *>(p)[4 * j + k]; }
+    __device__ __forceinline__ void set1(int64_t j, int k, float v) const { reinterpret_cast<float *>(p)[4 * j + k] = v; }
+};
+template <> struct Spins<double> {
+    double *x;
+    int64_t n;
+    static constexpr int kWords = 3; // doubles per site
+    __device__ __forceinline__ V3<double> get(int64_t j) const { return {x[j], x[n + j], x[2 * n + j]}; }
+    __device__ __forceinline__ void set(int64_t j, V3<double> s) const {
+        x[j] = s.x;
+        x[n + j] = s.y;
+        x[2 * n + j] = s.z;
+    }
+    __device__ __forceinline__ double get1(int64_t j, int k) const { return x[k * n + j]; }
+    __device__ __forceinline__ void set1(int64_t j, int k, double v) const { x[k * n + j] = v; }
+};
+// Replica r of a spin array of Np device sites per replica.
+__host__ __device__ __forceinline__ Spins<float> spins_of(float *base, int64_t Np, int64_t r) {
+    return {reinterpret_cast<float4 *>(base) + r * Np};
+}
+__host__ __device__ __forceinline__ Spins<double> spins_of(double *base, int64_t Np, int64_t r) {
+    return {base + r * 3 * Np, Np};
+}
+
 // Fields on site d from its partners, split by term order, without onsite,
 // self loops or the Zeeman field:
 //   hb = sum_n J_n s_j (bilinear), hc_a = sum C[a,b,c] s_j,b s_k,c,
 //   hq_a = sum R[a,b,c,d] s_j,b s_k,c s_l,d  (hamiltonian.jl:24-65).
-template <typename R, typename Idx, bool CUB, bool QUA>
-__device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R> &cf, const R *__restrict__ x,
-                                               const R *__restrict__ y, const R *__restrict__ z, int64_t d, int b,
+// SV is a spin view with get(j) (Spins<R> or a shared-memory view).
+template <typename R, typename Idx, bool CUB, bool QUA, class SV>
+__device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b,
                                                V3<R> &hb, V3<R> &hc, V3<R> &hq) {
     hb = {R(0), R(0), R(0)};
     hc = {R(0), R(0), R(0)};
@@ -86,7 +124,8 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     for (int t = 0; t < tb.W2; t++) {
         const int64_t j = tb.p2[t * Np + d];
         const R *M = cf.mats + 9 * cf.c2[b * tb.W2 + t];
-        const R sx = x[j], sy = y[j], sz = z[j];
+        const V3<R> sj = sv.get(j);
+        const R sx = sj.x, sy = sj.y, sz = sj.z;
         hb.x += M[0] * sx + M[1] * sy + M[2] * sz;
         hb.y += M[3] * sx + M[4] * sy + M[5] * sz;
         hb.z += M[6] * sx + M[7] * sy + M[8] * sz;
@@ -95,7 +134,8 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
         for (int t = 0; t < tb.W3; t++) {
             const int64_t j = tb.p3[(2 * t) * Np + d], k = tb.p3[(2 * t + 1) * Np + d];
             const R *C = cf.cubs + 27 * cf.c3[b * tb.W3 + t];
-            const R a0 = x[j], a1 = y[j], a2 = z[j], b0 = x[k], b1 = y[k], b2 = z[k];
+            const V3<R> sj = sv.get(j), sk = sv.get(k);
+            const R a0 = sj.x, a1 = sj.y, a2 = sj.z, b0 = sk.x, b1 = sk.y, b2 = sk.z;
             R o[9] = {a0 * b0, a0 * b1, a0 * b2, a1 * b0, a1 * b1, a1 * b2, a2 * b0, a2 * b1, a2 * b2};
             R sx = 0, sy = 0, sz = 0;
 #pragma unroll
@@ -113,7 +153,8 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
         for (int t = 0; t < tb.W4; t++) {
             const int64_t j = tb.p4[(3 * t) * Np + d], k = tb.p4[(3 * t + 1) * Np + d], l = tb.p4[(3 * t + 2) * Np + d];
             const R *Q = cf.quas + 81 * cf.c4[b * tb.W4 + t];
-            const R a[3] = {x[j], y[j], z[j]}, bb[3] = {x[k], y[k], z[k]}, c[3] = {x[l], y[l], z[l]};
+            const V3<R> sj = sv.get(j), sk = sv.get(k), sl = sv.get(l);
+            const R a[3] = {sj.x, sj.y, sj.z}, bb[3] = {sk.x, sk.y, sk.z}, c[3] = {sl.x, sl.y, sl.z};
             R sx = 0, sy = 0, sz = 0;
 #pragma unroll
             for (int p = 0; p < 3; p++)
@@ -143,12 +184,11 @@ template <typename R> __device__ __forceinline__ V3<R> matvec(const R *M, V3<R> 
 template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 // get_local_field (hamiltonian.jl:3-67): 2 O s + (self loops) + partners - h.
-template <typename R, typename Idx, bool CUB, bool QUA>
-__device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const R *x, const R *y,
-                                             const R *z, int64_t d, int b) {
+template <typename R, typename Idx, bool CUB, bool QUA, class SV>
+__device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b) {
     V3<R> hb, hc, hq;
-    partner_fields<R, Idx, CUB, QUA>(tb, cf, x, y, z, d, b, hb, hc, hq);
-    const V3<R> s = {x[d], y[d], z[d]};
+    partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
+    const V3<R> s = sv.get(d);
     const V3<R> os = matvec(cf.O + 9 * b, s), ps = matvec(cf.P + 9 * b, s);
     const R *h = cf.h + 3 * b;
     return {R(2) * os.x + ps.x + hb.x + hc.x + hq.x - h[0], R(2) * os.y + ps.y + hb.y + hc.y + hq.y - h[1],
@@ -171,12 +211,12 @@ __device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn
 
 // Contribution of site d to total_energy (hamiltonian.jl:70-132):
 // -s.h + s.O.s + (s.hb + s.P.s)/2 + s.hc/3 + s.hq/4.
-template <typename R, typename Idx, bool CUB, bool QUA>
-__device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const R *x, const R *y,
-                                                    const R *z, int64_t d, int b) {
+template <typename R, typename Idx, bool CUB, bool QUA, class SV>
+__device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d,
+                                                    int b) {
     V3<R> hb, hc, hq;
-    partner_fields<R, Idx, CUB, QUA>(tb, cf, x, y, z, d, b, hb, hc, hq);
-    const V3<R> s = {x[d], y[d], z[d]};
+    partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
+    const V3<R> s = sv.get(d);
     const R *h = cf.h + 3 * b;
     const R eo = dot(s, matvec(cf.O + 9 * b, s));
     const R ep = dot(s, matvec(cf.P + 9 * b, s));

@@ -18,12 +18,8 @@ constexpr int GB = 256; // block size of the global-path kernels
 
 // ------------------------------------------------------------ global path
 
-template <typename R> struct Ptrs {
-    R *x, *y, *z;
-};
-template <typename R> __device__ __forceinline__ Ptrs<R> replica(const SysArgs<R> &a, int r) {
-    R *x = a.spins + (int64_t)r * 3 * a.tb.Np;
-    return {x, x + a.tb.Np, x + 2 * a.tb.Np};
+template <typename R> __device__ __forceinline__ Spins<R> replica(const SysArgs<R> &a, int r) {
+    return spins_of(a.spins, a.tb.Np, r);
 }
 
 // One Metropolis colour step: every site of the class proposes once
@@ -33,7 +29,7 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
                                                      int chain_lo, int kind, uint32_t msweep, double T_override) {
     const int r = chain_lo + blockIdx.y;
     const int c = a.chain_base + r;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int slot = cs.slot_of[c];
     const double T = T_override > 0 ? T_override : cs.T_slot[slot];
     const R sigma = (R)cs.sigma_slot[slot];
@@ -43,19 +39,17 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
         const int64_t d = start + i;
         const int b = a.tb.pat[d];
         V3<R> hb, hc, hq;
-        partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b, hb, hc, hq);
+        partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
         const R *h = a.cf.h + 3 * b;
         const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
-        const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+        const V3<R> s = p.get(d);
         const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1);
         const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
         bool accept = dE < R(0);
         if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(-dE / (R)T);
         if (accept) {
-            p.x[d] = sn.x;
-            p.y[d] = sn.y;
-            p.z[d] = sn.z;
+            p.set(d, sn);
             acc = 1;
         }
     }
@@ -67,35 +61,31 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
     const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (i >= count) return;
     const int64_t d = start + i;
     const int b = a.tb.pat[d];
-    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
-    const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+    const V3<R> s = p.get(d);
     const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
-    p.x[d] = -s.x + proj * H.x;
-    p.y[d] = -s.y + proj * H.y;
-    p.z[d] = -s.z + proj * H.z;
+    p.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
 }
 
 // deterministic_updates! body (monte_carlo.jl:205-210) on one colour class.
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
     const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (i >= count) return;
     const int64_t d = start + i;
     const int b = a.tb.pat[d];
-    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
     const R n = Math<R>::sqrt_(H.x * H.x + H.y * H.y + H.z * H.z);
-    p.x[d] = -H.x / n * a.S;
-    p.y[d] = -H.y / n * a.S;
-    p.z[d] = -H.z / n * a.S;
+    p.set(d, {-H.x / n * a.S, -H.y / n * a.S, -H.z / n * a.S});
 }
 
 // Per-block partial sums of total_energy (hamiltonian.jl:70-132).
@@ -103,12 +93,12 @@ template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, double *part) {
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     double e = 0.0;
     if (d < a.tb.Np && a.dev2ref[d] >= 0) {
         const int b = a.tb.pat[d];
-        e = site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b);
+        e = site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     }
     e = block_sum<GB>(e, scratch);
     if (threadIdx.x == 0) part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = e;
@@ -118,13 +108,14 @@ __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, 
 template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArgs<R> a, int chain_lo, double *part) {
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     double mx = 0, my = 0, mz = 0;
     if (d < a.tb.Np) { // padding holds zero spins
-        mx = p.x[d];
-        my = p.y[d];
-        mz = p.z[d];
+        const V3<R> s = p.get(d);
+        mx = s.x;
+        my = s.y;
+        mz = s.z;
     }
     mx = block_sum<GB>(mx, scratch);
     my = block_sum<GB>(my, scratch);
@@ -176,79 +167,76 @@ __global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, d
     }
 }
 
-// Probe record: energy of the last Metropolis sweep and |M|, by slot.
-__global__ void k_probe_record(ChainState cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
-                               int n_slots) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    const int c = chain_first + q;
-    const int slot = cs.slot_of[c];
-    if (rec_E) rec_E[k * n_slots + slot] = cs.E_chain[c];
-    if (rec_M) rec_M[k * n_slots + slot] = cs.M_chain[c];
-}
-
-// Replica exchange of one lattice's slots (monte_carlo.jl:308-349): at
-// iteration `it` pairs (a, a+1) with a = (it/swap_rate) % 2 + 2m; the even
-// slot of the pair decides with probability min(1, exp(dbeta * dE)); an
-// accepted exchange swaps which replica sits in the two slots.
-__global__ void k_swap(ChainState cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
-                       uint32_t k0, uint32_t k1) {
-    const int phase = (int)((it / swap_rate) % 2);
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const int a = phase + 2 * m, b = a + 1;
-    if (b >= n_rep) return;
-    const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
-    const int sa = slot_base + a, sb = slot_base + b;
-    const int se = slot_base + ev, so = slot_base + od;
-    const double Te = cs.T_slot[se], To = cs.T_slot[so];
-    const double Ee = cs.E_chain[cs.chain_of[se]], Eo = cs.E_chain[cs.chain_of[so]];
-    const double delta_beta = (1 / To - 1 / Te);
-    const double delta_E = (Eo - Ee);
-    const double x = exp(delta_beta * delta_E);
-    // counter (pair, iteration low word, lattice id ^ iteration high word, SWAP)
-    const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, sys_id ^ (uint32_t)(it >> 32), PURPOSE_SWAP, k0, k1);
-    if (u53(w.x, w.y) < (x < 1.0 ? x : 1.0)) {
-        const int ca = cs.chain_of[sa], cb = cs.chain_of[sb];
-        cs.chain_of[sa] = cb;
-        cs.chain_of[sb] = ca;
-        cs.slot_of[cb] = sa;
-        cs.slot_of[ca] = sb;
-        cs.exch_slot[sa] += 1;
-        cs.exch_slot[sb] += 1;
+// Replica exchange of every lattice of the context followed by the probe
+// record of the same iteration (monte_carlo.jl:308-349 then :368-370): one
+// block per lattice; the pairs of a lattice are decided in parallel (they
+// are disjoint), then, after the block barrier, every slot records the energy
+// and |M| of the replica that now sits in it.  kq < 0: no record.
+__global__ void k_exchange(ChainState cs, const int2 *lattices, int64_t it, int swap_rate, uint32_t k0, uint32_t k1,
+                           int do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots) {
+    const int sys = blockIdx.x;
+    const int slot_base = lattices[sys].x, n_rep = lattices[sys].y;
+    if (do_swap && n_rep >= 2) {
+        const int phase = (int)((it / swap_rate) % 2);
+        for (int m = threadIdx.x; phase + 2 * m + 1 < n_rep; m += blockDim.x) {
+            const int a = phase + 2 * m, b = a + 1;
+            const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
+            const int sa = slot_base + a, sb = slot_base + b;
+            const int se = slot_base + ev, so = slot_base + od;
+            const double Te = cs.T_slot[se], To = cs.T_slot[so];
+            const double Ee = cs.E_chain[cs.chain_of[se]], Eo = cs.E_chain[cs.chain_of[so]];
+            const double x = exp((1 / To - 1 / Te) * (Eo - Ee));
+            const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, (uint32_t)sys ^ (uint32_t)(it >> 32), PURPOSE_SWAP,
+                                       k0, k1);
+            if (u53(w.x, w.y) < (x < 1.0 ? x : 1.0)) {
+                const int ca = cs.chain_of[sa], cb = cs.chain_of[sb];
+                cs.chain_of[sa] = cb;
+                cs.chain_of[sb] = ca;
+                cs.slot_of[cb] = sa;
+                cs.slot_of[ca] = sb;
+                cs.exch_slot[sa] += 1;
+                cs.exch_slot[sb] += 1;
+            }
+        }
+    }
+    if (kq < 0) return;
+    __syncthreads();
+    for (int q = threadIdx.x; q < n_rep; q += blockDim.x) {
+        const int slot = slot_base + q, c = cs.chain_of[slot];
+        if (rec_E) rec_E[kq * n_slots + slot] = cs.E_chain[c];
+        if (rec_M) rec_M[kq * n_slots + slot] = cs.M_chain[c];
     }
 }
 
 // Reference layout (interleaved FP64, reference order) <-> device order.
-template <typename R> __global__ void k_scatter(SysArgs<R> a, int chain_lo, const double *src) {
-    const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
-    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
-    if (d >= a.tb.Np) return;
-    const int64_t i = a.dev2ref[d];
-    if (i < 0) return;
-    const double *s = src + ((int64_t)blockIdx.y * a.n_real + i) * 3;
-    p.x[d] = (R)s[0];
-    p.y[d] = (R)s[1];
-    p.z[d] = (R)s[2];
+// One thread per element e = 3 i + k (site i, component k) of a slot's 3 x N
+// array, so the FP64 buffer is read (scatter) or written (gather) once and
+// contiguously across a warp; `buf` may be device memory or pinned host
+// memory mapped into the device's address space.  The slot's replica is
+// looked up on the device (chain_of), so a batch of slots is one launch
+// whatever the exchange permutation.
+template <typename R>
+__global__ void k_scatter(SysArgs<R> a, const int32_t *chain_of, int slot_first, const double *src) {
+    const int64_t e = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (e >= 3 * a.n_real) return;
+    const int r = chain_of[slot_first + blockIdx.y] - a.chain_base;
+    const int64_t i = e / 3;
+    replica(a, r).set1(a.ref2dev[i], (int)(e - 3 * i), (R)src[(int64_t)blockIdx.y * 3 * a.n_real + e]);
 }
 
-template <typename R> __global__ void k_gather(SysArgs<R> a, int chain_lo, double *dst) {
-    const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
-    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
-    if (d >= a.tb.Np) return;
-    const int64_t i = a.dev2ref[d];
-    if (i < 0) return;
-    double *s = dst + ((int64_t)blockIdx.y * a.n_real + i) * 3;
-    s[0] = (double)p.x[d];
-    s[1] = (double)p.y[d];
-    s[2] = (double)p.z[d];
+template <typename R>
+__global__ void k_gather(SysArgs<R> a, const int32_t *chain_of, int slot_first, double *dst) {
+    const int64_t e = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (e >= 3 * a.n_real) return;
+    const int r = chain_of[slot_first + blockIdx.y] - a.chain_base;
+    const int64_t i = e / 3;
+    dst[(int64_t)blockIdx.y * 3 * a.n_real + e] = (double)replica(a, r).get1(a.ref2dev[i], (int)(e - 3 * i));
 }
 
 // Uniform spins from the INIT stream, counter (reference site, 0, chain, INIT).
 template <typename R> __global__ void k_random_spins(SysArgs<R> a, uint32_t k0, uint32_t k1) {
     const int r = blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (d >= a.tb.Np) return;
     const int64_t i = a.dev2ref[d];
@@ -260,18 +248,16 @@ template <typename R> __global__ void k_random_spins(SysArgs<R> a, uint32_t k0, 
     const double z = 2.0 * uz - 1.0;
     const double rr = sqrt(fmax(1.0 - z * z, 0.0));
     const double S = (double)a.S;
-    p.x[d] = (R)(S * (rr * cp));
-    p.y[d] = (R)(S * (rr * sp));
-    p.z[d] = (R)(S * z);
+    p.set(d, {(R)(S * (rr * cp)), (R)(S * (rr * sp)), (R)(S * z)});
 }
 
 template <typename R, bool CUB, bool QUA> __global__ void k_local_field(SysArgs<R> a, int r, double *out) {
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (d >= a.tb.Np) return;
     const int64_t i = a.dev2ref[d];
     if (i < 0) return;
-    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, a.tb.pat[d]);
+    const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, a.tb.pat[d]);
     out[3 * i] = (double)H.x;
     out[3 * i + 1] = (double)H.y;
     out[3 * i + 2] = (double)H.z;
@@ -279,40 +265,39 @@ template <typename R, bool CUB, bool QUA> __global__ void k_local_field(SysArgs<
 
 template <typename R, bool CUB, bool QUA>
 __global__ void k_energy_diff(SysArgs<R> a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE) {
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t q = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (q >= n) return;
     const int64_t d = a.ref2dev[sites[q]];
     const int b = a.tb.pat[d];
     V3<R> hb, hc, hq;
-    partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p.x, p.y, p.z, d, b, hb, hc, hq);
+    partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
     const R *h = a.cf.h + 3 * b;
     const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
-    const V3<R> s = {p.x[d], p.y[d], p.z[d]};
+    const V3<R> s = p.get(d);
     const V3<R> sn = {(R)ns[3 * q], (R)ns[3 * q + 1], (R)ns[3 * q + 2]};
     dE[q] = (double)delta_e<R>(a.cf, b, s, sn, hext);
 }
 
 template <typename R> __global__ void k_renorm(SysArgs<R> a, int chain_lo) {
     const int r = chain_lo + blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (d >= a.tb.Np || a.dev2ref[d] < 0) return;
-    const R x = p.x[d], y = p.y[d], z = p.z[d];
-    const R n2 = x * x + y * y + z * z;
+    const V3<R> s = p.get(d);
+    const R n2 = s.x * s.x + s.y * s.y + s.z * s.z;
     if (n2 == R(0)) return;
     const R f = a.S * Math<R>::rsqrt_(n2);
-    p.x[d] = x * f;
-    p.y[d] = y * f;
-    p.z[d] = z * f;
+    p.set(d, {s.x * f, s.y * f, s.z * f});
 }
 
 template <typename R> __global__ void k_drift(SysArgs<R> a, unsigned int *bits) {
     const int r = blockIdx.y;
-    const Ptrs<R> p = replica(a, r);
+    const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (d >= a.tb.Np || a.dev2ref[d] < 0) return;
-    const double x = p.x[d], y = p.y[d], z = p.z[d];
+    const V3<R> s = p.get(d);
+    const double x = s.x, y = s.y, z = s.z;
     const double S = (double)a.S;
     const float e = (float)(fabs(sqrt(x * x + y * y + z * z) - S) / (S != 0 ? S : 1.0));
     atomicMax(bits, __float_as_uint(e));
@@ -382,23 +367,21 @@ void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, 
     k_after_metro<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, kind, (double)n_sites, last_acc);
 }
 
-void launch_probe_record(const ChainState &cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
-                         int n_slots, cudaStream_t st) {
-    if (n <= 0) return;
-    k_probe_record<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, rec_E, rec_M, k, n_slots);
+void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,
+                     uint32_t k1, bool do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots, cudaStream_t st) {
+    k_exchange<<<n_lattices, 256, 0, st>>>(cs, lattices, it, swap_rate, k0, k1, do_swap ? 1 : 0, rec_E, rec_M, kq,
+                                           n_slots);
 }
 
-void launch_swap(const ChainState &cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
-                 uint32_t k0, uint32_t k1, cudaStream_t st) {
-    const int pairs = n_rep / 2 + 1;
-    k_swap<<<(pairs + 127) / 128, 128, 0, st>>>(cs, slot_base, n_rep, it, swap_rate, sys_id, k0, k1);
+template <typename R>
+void launch_scatter(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, const double *src,
+                    cudaStream_t st) {
+    k_scatter<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, src);
 }
-
-template <typename R> void launch_scatter(const SysArgs<R> &a, int chain_lo, int n_chains, const double *src, cudaStream_t st) {
-    k_scatter<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo, src);
-}
-template <typename R> void launch_gather(const SysArgs<R> &a, int chain_lo, int n_chains, double *dst, cudaStream_t st) {
-    k_gather<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo, dst);
+template <typename R>
+void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, double *dst,
+                   cudaStream_t st) {
+    k_gather<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, dst);
 }
 template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st) {
     k_random_spins<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, k0, k1);
@@ -428,8 +411,8 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
     template void launch_det_colour<R>(const SysArgs<R> &, int64_t, int64_t, int, int, cudaStream_t);                 \
     template void launch_energy<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \
     template void launch_magnet<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \
-    template void launch_scatter<R>(const SysArgs<R> &, int, int, const double *, cudaStream_t);                      \
-    template void launch_gather<R>(const SysArgs<R> &, int, int, double *, cudaStream_t);                             \
+    template void launch_scatter<R>(const SysArgs<R> &, const int32_t *, int, int, const double *, cudaStream_t);     \
+    template void launch_gather<R>(const SysArgs<R> &, const int32_t *, int, int, double *, cudaStream_t);            \
     template void launch_random_spins<R>(const SysArgs<R> &, uint32_t, uint32_t, cudaStream_t);                       \
     template void launch_local_field<R>(const SysArgs<R> &, int, double *, cudaStream_t);                             \
     template void launch_energy_diff<R>(const SysArgs<R> &, int, int64_t, const int64_t *, const double *, double *,  \

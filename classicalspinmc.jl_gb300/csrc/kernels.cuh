@@ -59,6 +59,9 @@ template <typename R> struct ResSys {
     // 16-bit partners, sentinel-padded): p2v[i] for one CTA per replica,
     // q2v[rank][i] for clusters; used by the specialised kernel
     const uint4 *p2v, *q2v;
+    // nonzero: the specialised kernel stages the CTA's partner words in
+    // shared memory too (they fit beside the spins)
+    int32_t pv_stage;
 };
 constexpr int RESIDENT_CLUSTER_MAX = 4;
 
@@ -70,10 +73,17 @@ constexpr int RESIDENT_CLUSTER_MAX = 4;
 struct ResidentSel {
     bool fast;
     int bil, ons;
+    int width; // specialised kernel: bilinear partners per site (4, 6 or 8)
     bool cub, qua;
     int cl; // CTAs per replica (thread-block cluster size; 1 = no cluster)
 };
 constexpr int RESIDENT_WMAX = 8; // bilinear slots per site of the specialised kernel
+// Threads per CTA at most of a resident kernel (its launch bound): 1024 for
+// the specialised kernel with scalar couplings and at most diagonal onsite
+// terms (64 registers per thread suffice), else 512.
+__host__ __device__ constexpr int resident_max_threads(bool fast, int bil, int ons) {
+    return fast && bil == 0 && ons < 2 ? 1024 : 512;
+}
 
 // The sweep schedule of one resident launch (see csmc_run_params).
 struct RunDesc {
@@ -86,7 +96,6 @@ struct RunDesc {
     double sigma0;
     uint32_t msweep0;         // Metropolis sweep counter at the first Metropolis sweep
     int32_t or_rate, swap_rate, probe_rate, kind;
-    int32_t pending_probe;    // record the probe of iteration it0-1 first
     int32_t reset_sigma;      // sigma <- sigma0 before the first sweep
     int32_t n_slots;
     int32_t renorm_every;     // single precision: renormalise every k sweeps

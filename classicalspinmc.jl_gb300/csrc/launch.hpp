@@ -26,13 +26,19 @@ void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int 
                    cudaStream_t st);
 void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double *last_acc,
                         cudaStream_t st);
-void launch_probe_record(const ChainState &cs, int chain_first, int n, double *rec_E, double *rec_M, int64_t k,
-                         int n_slots, cudaStream_t st);
-void launch_swap(const ChainState &cs, int slot_base, int n_rep, int64_t it, int swap_rate, uint32_t sys_id,
-                 uint32_t k0, uint32_t k1, cudaStream_t st);
+// Exchange of every lattice (lattices[k] = {first slot, replicas}) at
+// iteration `it`, then, if kq >= 0, probe record kq of every slot.
+void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,
+                     uint32_t k1, bool do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots, cudaStream_t st);
+// FP64 reference layout <-> device order for slots [slot_first, +n_slots) of
+// one lattice (the replica of each slot looked up in chain_of on the device);
+// buf holds n_slots consecutive 3 x N arrays.
 template <typename R>
-void launch_scatter(const SysArgs<R> &a, int chain_lo, int n_chains, const double *src, cudaStream_t st);
-template <typename R> void launch_gather(const SysArgs<R> &a, int chain_lo, int n_chains, double *dst, cudaStream_t st);
+void launch_scatter(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, const double *src,
+                    cudaStream_t st);
+template <typename R>
+void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, double *dst,
+                   cudaStream_t st);
 template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st);
 template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st);
 template <typename R>
@@ -46,6 +52,8 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
                             const ResidentSel &sel, cudaStream_t st);
 // CTAs (cl = 1) or clusters (cl > 1) of the selected resident kernel that fit on the device at once
 template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms);
+// static shared memory of the selected resident kernel in bytes (-1: query failed)
+template <typename R> int resident_static_smem(const ResidentSel &sel);
 
 // Reference-layout tables of one lattice for the replay kernel (exact.cu):
 // per reference site, N2/N3/N4 term entries with 0-based partners (-1 absent).

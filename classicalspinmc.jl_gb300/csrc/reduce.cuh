@@ -21,6 +21,24 @@ template <int NT> __device__ __forceinline__ double block_sum(double v, double *
     return t;
 }
 
+// The same for a block of any multiple of 32 threads (blockDim.x); scratch
+// needs blockDim.x/32 doubles.
+__device__ __forceinline__ double block_sum_any(double v, double *scratch) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) scratch[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? scratch[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+
 __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

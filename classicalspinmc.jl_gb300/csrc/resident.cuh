@@ -5,7 +5,13 @@
 // Metropolis sweeps, the FP64 total energy, probes, spin renormalisation):
 // it is staged in with bulk TMA copies (cp.async.bulk, completion on an
 // mbarrier, bounded wait), updated colour class by colour class with a
-// barrier between classes, and written back once.
+// barrier between classes, and written back once (single precision: bulk
+// TMA stores).
+//
+// Shared-memory layout: the replica's spins in the device layout (single
+// precision: one float4 per site; double: x | y | z blocks), then, for the
+// specialised kernel when it fits, the packed partner words of the CTA's
+// sites (one 16-byte word per site, also staged by TMA).
 //
 // A replica lives either in one CTA (CL = 1; a work list hands replicas out,
 // largest first) or in a thread-block cluster of CL CTAs (CL = 2, 4): rank k
@@ -14,12 +20,16 @@
 // between colour classes is a cluster barrier.  This spreads few replicas
 // over more SMs.
 //
+// The block size is chosen at launch (a multiple of 32, at most NT) so that
+// every thread updates the same number of sites between two barriers.
+//
 // Two physics policies share the driver loop:
 //  * ResidentGeneric: per-site pattern, cubic and quartic terms (device.cuh);
 //  * ResidentFast: no cubic/quartic terms and one basis per colour class; the
 //    couplings of a colour class are loaded once per class into registers
-//    (scalar couplings) or staged in shared memory (general 3x3), and the
-//    onsite matrices are specialised to none / diagonal / general.
+//    (scalar couplings) or staged in shared memory (general 3x3), the onsite
+//    matrices are specialised to none / diagonal / general, and the number of
+//    bilinear partners per site W (4, 6 or 8) is a compile-time constant.
 #pragma once
 
 #include "kernels.cuh"
@@ -52,6 +62,16 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
+}
+// Bulk TMA copy shared -> global in the current bulk group.
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Close the bulk group and wait until all of its copies have completed.
+__device__ __forceinline__ void bulk_commit_and_wait() {
+    asm volatile("cp.async.bulk.commit_group;\n\tcp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 // Bounded wait on an mbarrier phase: gives up after a fixed number of polls
@@ -88,25 +108,24 @@ __device__ __forceinline__ uint32_t map_rank(uint32_t saddr, uint32_t rank) {
     asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
     return r;
 }
-// generic address of the same shared variable in CTA `rank` (plain loads
-// through it reach that CTA's shared memory)
-template <typename T> __device__ __forceinline__ const T *map_rank_generic(const T *p, uint32_t rank) {
-    uint64_t r;
-    asm("mapa.u64 %0, %1, %2;" : "=l"(r) : "l"((uint64_t)p), "r"(rank));
-    return reinterpret_cast<const T *>(r);
-}
-// Loads from another CTA's shared memory.  Volatile keeps them between the
-// (volatile, memory-clobbering) barriers that order them; no memory clobber,
-// since within a colour class they read sites no thread writes.
-__device__ __forceinline__ float ld_cluster(uint32_t a, float) {
-    float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a));
-    return v;
-}
+// Loads through the shared::cluster window (this CTA's or another rank's
+// shared memory).  Volatile keeps them between the (volatile,
+// memory-clobbering) barriers that order them; no memory clobber, since
+// within a colour class they read sites no thread writes.
 __device__ __forceinline__ double ld_cluster(uint32_t a, double) {
     double v;
     asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a));
     return v;
+}
+// One site's spin through the cluster window: float4 at a (single
+// precision) or x, y, z at a, a + comp, a + 2 comp (double precision).
+__device__ __forceinline__ V3<float> cluster_spin(uint32_t a, uint32_t, float) {
+    float x, y, z, w;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(x), "=f"(y), "=f"(z), "=f"(w) : "r"(a));
+    return {x, y, z};
+}
+__device__ __forceinline__ V3<double> cluster_spin(uint32_t a, uint32_t comp, double) {
+    return {ld_cluster(a, 0.0), ld_cluster(a + comp, 0.0), ld_cluster(a + 2 * comp, 0.0)};
 }
 
 // Remote arrive on the mbarrier at shared::cluster address `a` (release at
@@ -126,10 +145,31 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t pa
     return ok != 0;
 }
 
+// Bytes of one site in shared memory per spin component block: 16 (float4
+// sites) or 8 (one double of a component block).
+template <typename R> constexpr uint32_t site_stride() { return sizeof(R) == 4 ? 16u : 8u; }
+// Shared-memory view of `n` local sites starting at `base`.
+__device__ __forceinline__ Spins<float> smem_spins(unsigned char *base, int64_t) {
+    return {reinterpret_cast<float4 *>(base)};
+}
+__device__ __forceinline__ Spins<double> smem_spins_d(unsigned char *base, int64_t n) {
+    return {reinterpret_cast<double *>(base), n};
+}
+template <typename R> __device__ __forceinline__ Spins<R> local_spins(unsigned char *base, int64_t n) {
+    if constexpr (sizeof(R) == 4) return smem_spins(base, n);
+    else return smem_spins_d(base, n);
+}
+__device__ __forceinline__ const void *spin_base(const Spins<float> &s) { return s.p; }
+__device__ __forceinline__ const void *spin_base(const Spins<double> &s) { return s.x; }
+// Bytes of the spin part of shared memory for n local sites.
+template <typename R> __host__ __device__ constexpr int64_t spin_smem_bytes(int64_t n) {
+    return sizeof(R) == 4 ? 16 * n : 24 * n;
+}
+
 // Block (CL = 1) or cluster barrier and sums; totals valid in thread 0 of
 // every CTA, identical on all ranks (same summation order).
-template <int NT, int CL> struct Sync {
-    double *scratch, *red; // scratch: NT/32 doubles; red: 3 doubles (cluster exchange)
+template <int CL> struct Sync {
+    double *scratch, *red; // scratch: 32 doubles; red: 3 doubles (cluster exchange)
     uint64_t *pbar;        // phase mbarrier of this CTA (CL arrivals per phase)
     uint32_t *pphase;      // its current phase parity (thread 0)
     int *error_flag;
@@ -155,7 +195,7 @@ template <int NT, int CL> struct Sync {
         }
     }
     __device__ double sum(double v) const {
-        double t = block_sum<NT>(v, scratch);
+        double t = block_sum_any(v, scratch);
         if (CL == 1) return t;
         if (threadIdx.x == 0) red[0] = t;
         cluster_sync_all();
@@ -166,9 +206,9 @@ template <int NT, int CL> struct Sync {
         return tot;
     }
     __device__ void sum3(double &a, double &b, double &c) const {
-        a = block_sum<NT>(a, scratch);
-        b = block_sum<NT>(b, scratch);
-        c = block_sum<NT>(c, scratch);
+        a = block_sum_any(a, scratch);
+        b = block_sum_any(b, scratch);
+        c = block_sum_any(c, scratch);
         if (CL == 1) return;
         if (threadIdx.x == 0) {
             red[0] = a;
@@ -190,10 +230,10 @@ template <int NT, int CL> struct Sync {
 };
 
 // Local part of a replica in this CTA and the iteration over its colour class.
-template <typename R, int NT, int CL> struct ResidentCommon {
+template <typename R, int CL> struct ResidentCommon {
     const ResSys<R> &S;
-    R *x, *y, *z; // local shared-memory arrays (stride Npl when CL > 1, else Np)
-    Sync<NT, CL> sy;
+    Spins<R> sp; // this CTA's sites in shared memory (local indices)
+    Sync<CL> sy;
     int c, slot, rank;
     R *scoef;
 
@@ -212,10 +252,11 @@ template <typename R, int NT, int CL> struct ResidentCommon {
         double mx = 0, my = 0, mz = 0;
         for (int col = 0; col < S.n_colours; col++) { // the sites of this CTA only
             const int st = col_begin(col), n = col_size(col);
-            for (int i = threadIdx.x; i < n; i += NT) {
-                mx += x[st + i];
-                my += y[st + i];
-                mz += z[st + i];
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const V3<R> s = sp.get(st + i);
+                mx += s.x;
+                my += s.y;
+                mz += s.z;
             }
         }
         sy.sum3(mx, my, mz);
@@ -225,47 +266,44 @@ template <typename R, int NT, int CL> struct ResidentCommon {
     __device__ void renormalize() const {
         for (int col = 0; col < S.n_colours; col++) {
             const int st = col_begin(col), n = col_size(col);
-            for (int i = threadIdx.x; i < n; i += NT) {
-                const int d = st + i;
-                const R a = x[d], b = y[d], cc = z[d];
-                const R n2 = a * a + b * b + cc * cc;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const V3<R> s = sp.get(st + i);
+                const R n2 = s.x * s.x + s.y * s.y + s.z * s.z;
                 if (n2 == R(0)) continue;
                 const R f = S.S * Math<R>::rsqrt_(n2);
-                x[d] = a * f;
-                y[d] = b * f;
-                z[d] = cc * f;
+                sp.set(st + i, {s.x * f, s.y * f, s.z * f});
             }
         }
         sy.bar();
     }
 };
 
-template <typename R, bool CUB, bool QUA, int NT, int CL> struct ResidentGeneric : ResidentCommon<R, NT, CL> {
+template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : ResidentCommon<R, CL> {
     static_assert(CL == 1, "the generic resident kernel runs one CTA per replica");
+    static constexpr int kMaxThreads = 512; // 128 registers per thread
     static constexpr int kCoefSmem = 1;
-    using B = ResidentCommon<R, NT, CL>;
+    static constexpr bool kPartnerWords = false;
+    using B = ResidentCommon<R, CL>;
     using B::c;
     using B::S;
-    using B::x;
-    using B::y;
-    using B::z;
-    __device__ ResidentGeneric(const ResSys<R> &s, R *x_, R *y_, R *z_, Sync<NT, CL> sy_, int c_, int slot_, int rk,
-                               R *coef)
-        : B{s, x_, y_, z_, sy_, c_, slot_, rk, coef} {}
+    using B::sp;
+    __device__ ResidentGeneric(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
+                               const uint4 *)
+        : B{s, sp_, sy_, c_, slot_, rk, coef} {}
     __device__ void prepare() const {}
 
     __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
         unsigned acc = 0;
         for (int col = 0; col < S.n_colours; col++) {
             const int st = (int)S.col_start[col], n = (int)S.col_count[col];
-            for (int i = threadIdx.x; i < n; i += NT) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
                 const int b = S.tb.pat[d];
                 V3<R> hb, hc, hq;
-                partner_fields<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, b, hb, hc, hq);
+                partner_fields<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, b, hb, hc, hq);
                 const R *h = S.cf.h + 3 * b;
                 const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
-                const V3<R> s = {x[d], y[d], z[d]};
+                const V3<R> s = sp.get(d);
                 const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
                 const R dE = delta_e<R>(S.cf, b, s, sn, hext);
@@ -275,9 +313,7 @@ template <typename R, bool CUB, bool QUA, int NT, int CL> struct ResidentGeneric
                     accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
                 }
                 if (accept) {
-                    x[d] = sn.x;
-                    y[d] = sn.y;
-                    z[d] = sn.z;
+                    sp.set(d, sn);
                     acc++;
                 }
             }
@@ -289,15 +325,13 @@ template <typename R, bool CUB, bool QUA, int NT, int CL> struct ResidentGeneric
     __device__ void or_sweep() const {
         for (int col = 0; col < S.n_colours; col++) {
             const int st = (int)S.col_start[col], n = (int)S.col_count[col];
-            for (int i = threadIdx.x; i < n; i += NT) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
+                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, S.tb.pat[d]);
                 if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
-                const V3<R> s = {x[d], y[d], z[d]};
+                const V3<R> s = sp.get(d);
                 const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
-                x[d] = -s.x + proj * H.x;
-                y[d] = -s.y + proj * H.y;
-                z[d] = -s.z + proj * H.z;
+                sp.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
             }
             __syncthreads();
         }
@@ -307,56 +341,64 @@ template <typename R, bool CUB, bool QUA, int NT, int CL> struct ResidentGeneric
         double e = 0.0;
         for (int col = 0; col < S.n_colours; col++) {
             const int st = (int)S.col_start[col], n = (int)S.col_count[col];
-            for (int i = threadIdx.x; i < n; i += NT) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                e += site_energy_share<R, uint16_t, CUB, QUA>(S.tb, S.cf, x, y, z, d, S.tb.pat[d]);
+                e += site_energy_share<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, S.tb.pat[d]);
             }
         }
         return this->sy.sum(e);
     }
 };
 
-template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : ResidentCommon<R, NT, CL> {
+template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : ResidentCommon<R, CL> {
+    static_assert(W == 4 || W == 6 || W == 8, "partner widths 4, 6 and 8");
+    // scalar couplings and at most diagonal onsite terms fit 64 registers per
+    // thread (1024 threads); 3x3 couplings or general onsite terms get 128
+    static constexpr int kMaxThreads = (BIL == 0 && ONS < 2) ? 1024 : 512;
     static constexpr int WMAX = RESIDENT_WMAX;
     static constexpr int kCoefSmem = BIL ? CSMC_MAX_COLOURS * WMAX * 9 : 1;
-    using B = ResidentCommon<R, NT, CL>;
+    static constexpr bool kPartnerWords = true;
+    using B = ResidentCommon<R, CL>;
     using B::c;
     using B::rank;
     using B::S;
     using B::scoef;
-    using B::x;
-    using B::y;
-    using B::z;
-    const R *xr[CL]; // generic pointer to x in every rank (CL > 1; own rank: x itself)
+    using B::sp;
+    const uint4 *pv; // packed partner words of this CTA's sites, by local index (shared or global memory)
+    uint32_t rb[CL]; // shared::cluster address of local site 0 in every rank (CL > 1)
+    uint32_t comp;   // double precision: bytes between the x, y and z blocks
 
-    __device__ ResidentFast(const ResSys<R> &s, R *x_, R *y_, R *z_, Sync<NT, CL> sy_, int c_, int slot_, int rk,
-                            R *coef)
-        : B{s, x_, y_, z_, sy_, c_, slot_, rk, coef} {
+    __device__ ResidentFast(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
+                            const uint4 *pv_)
+        : B{s, sp_, sy_, c_, slot_, rk, coef}, pv(pv_) {
+        comp = (uint32_t)(S.Npl * sizeof(double));
         if (CL > 1) {
+            const uint32_t a = smem_u32(spin_base(sp));
 #pragma unroll
-            for (int r = 0; r < CL; r++) xr[r] = r == rk ? x_ : map_rank_generic<R>(x_, r);
+            for (int r = 0; r < CL; r++) rb[r] = map_rank(a, r);
         }
     }
 
-    // stage the 3x3 couplings of every colour class: scoef[(col*W + t)*9 + e]
+    // stage the 3x3 couplings of every colour class, zero for slots beyond
+    // the lattice's W2: scoef[(col*W + t)*9 + e]
     __device__ void prepare() const {
         if (BIL) {
-            const int W = S.tb.W2, n = S.n_colours * W * 9;
-            for (int k = threadIdx.x; k < n; k += NT) {
+            const int W2 = S.tb.W2, n = S.n_colours * W * 9;
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int col = k / (W * 9), rem = k - col * W * 9, t = rem / 9, e = rem - t * 9;
                 const int b = S.col_pattern[col];
-                scoef[k] = S.cf.mats[9 * S.cf.c2[b * W + t] + e];
+                scoef[k] = t < W2 ? S.cf.mats[9 * S.cf.c2[b * W2 + t] + e] : R(0);
             }
             __syncthreads();
         }
     }
 
-    // per colour class: slot scalars J, an onsite-class matrix m (from A, Q
-    // or E2) and the field h
-    __device__ __forceinline__ void load_coef(int col, const R *src, R (&J)[WMAX], R (&m)[9], V3<R> &h) const {
-        const int b = S.col_pattern[col], W = S.tb.W2;
+    // per colour class: slot scalars J (zero beyond the lattice's W2), an
+    // onsite-class matrix m (from A, Q or E2) and the field h
+    __device__ __forceinline__ void load_coef(int col, const R *src, R (&J)[W], R (&m)[9], V3<R> &h) const {
+        const int b = S.col_pattern[col], W2 = S.tb.W2;
 #pragma unroll
-        for (int t = 0; t < WMAX; t++) J[t] = (BIL == 0 && t < W) ? S.cf.Js[b * W + t] : R(0);
+        for (int t = 0; t < W; t++) J[t] = (BIL == 0 && t < W2) ? S.cf.Js[b * W2 + t] : R(0);
 #pragma unroll
         for (int k = 0; k < 9; k++) m[k] = ONS == 0 ? R(0) : src[9 * b + k];
         h = {S.cf.h[3 * b], S.cf.h[3 * b + 1], S.cf.h[3 * b + 2]};
@@ -368,83 +410,61 @@ template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : Re
         return matvec(m, s);
     }
 
-    __device__ __forceinline__ const R *rank_x(uint32_t own) const {
-        if (CL == 2) return own ? xr[1 % CL] : xr[0];
-        if (CL == 4) return own < 2 ? (own ? xr[1 % CL] : xr[0]) : (own == 2 ? xr[2 % CL] : xr[3 % CL]);
-        return xr[0];
-    }
-
-    __device__ __forceinline__ void accumulate(V3<R> &hb, int col, int t, const R (&J)[WMAX], R sx, R sy_,
-                                               R sz) const {
+    __device__ __forceinline__ void accumulate(V3<R> &hb, int col, int t, const R (&J)[W], V3<R> s) const {
         if (BIL == 0) {
-            hb.x += J[t] * sx;
-            hb.y += J[t] * sy_;
-            hb.z += J[t] * sz;
+            hb.x += J[t] * s.x;
+            hb.y += J[t] * s.y;
+            hb.z += J[t] * s.z;
         } else {
-            const R *M = scoef + (col * S.tb.W2 + t) * 9;
-            hb.x += M[0] * sx + M[1] * sy_ + M[2] * sz;
-            hb.y += M[3] * sx + M[4] * sy_ + M[5] * sz;
-            hb.z += M[6] * sx + M[7] * sy_ + M[8] * sz;
+            const R *M = scoef + (col * W + t) * 9;
+            hb.x += M[0] * s.x + M[1] * s.y + M[2] * s.z;
+            hb.y += M[3] * s.x + M[4] * s.y + M[5] * s.z;
+            hb.z += M[6] * s.x + M[7] * s.y + M[8] * s.z;
         }
     }
 
-    // unpack the 8 16-bit partners of a site from its packed word
-    static __device__ __forceinline__ void unpack(const uint4 w, uint32_t (&v)[WMAX]) {
-        v[0] = w.x & 0xFFFFu;
-        v[1] = w.x >> 16;
-        v[2] = w.y & 0xFFFFu;
-        v[3] = w.y >> 16;
-        v[4] = w.z & 0xFFFFu;
-        v[5] = w.z >> 16;
-        v[6] = w.w & 0xFFFFu;
-        v[7] = w.w >> 16;
+    // the spin of partner entry v: a local index (CL = 1) or
+    // (owner rank << 14) | owner-local index (CL > 1)
+    __device__ __forceinline__ V3<R> partner(uint32_t v) const {
+        if (CL == 1) return sp.get((int)v);
+        const uint32_t owner = v >> 14, local = v & 0x3FFFu;
+        uint32_t b = rb[0];
+        if (CL == 2) b = owner ? rb[1 % CL] : rb[0];
+        if (CL == 4)
+            b = (owner & 2u) ? ((owner & 1u) ? rb[3 % CL] : rb[2 % CL]) : ((owner & 1u) ? rb[1 % CL] : rb[0]);
+        return cluster_spin(b + local * site_stride<R>(), comp, R(0));
     }
 
-    // sum over bilinear slots of J_t s_j at local site i: the partner indices
-    // come in one 16-byte load, each partner spin is consumed as soon as it is
-    // loaded
-    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[WMAX], int i) const {
+    // sum over bilinear slots of J_t s_j at local site i: the partner entries
+    // come in one 16-byte word, every partner load is issued before use
+    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], int i) const {
+        const uint4 w = pv[i];
+        const uint32_t v[8] = {w.x & 0xFFFFu, w.x >> 16, w.y & 0xFFFFu, w.y >> 16,
+                               w.z & 0xFFFFu, w.z >> 16, w.w & 0xFFFFu, w.w >> 16};
+        V3<R> s[W];
+#pragma unroll
+        for (int t = 0; t < W; t++) s[t] = partner(v[t]);
         V3<R> hb = {R(0), R(0), R(0)};
-        const int W = S.tb.W2;
-        uint32_t v[WMAX];
-        if (CL == 1) {
-            unpack(S.p2v[i], v);
 #pragma unroll
-            for (int t = 0; t < WMAX; t++)
-                if (t < W) accumulate(hb, col, t, J, x[v[t]], y[v[t]], z[v[t]]);
-        } else {
-            const int Npl = S.Npl;
-            unpack(S.q2v[(size_t)rank * Npl + i], v);
-            // one path for every partner: a generic pointer into the owning
-            // CTA's shared memory (this CTA's or, through distributed shared
-            // memory, another rank's)
-#pragma unroll
-            for (int t = 0; t < WMAX; t++)
-                if (t < W) {
-                    const R *p = rank_x(v[t] >> 14) + (v[t] & 0x3FFFu);
-                    accumulate(hb, col, t, J, p[0], p[Npl], p[2 * Npl]);
-                }
-        }
+        for (int t = 0; t < W; t++) accumulate(hb, col, t, J, s[t]);
         return hb;
     }
 
     __device__ void or_sweep() const {
         for (int col = 0; col < S.n_colours; col++) {
-            R J[WMAX], a[9];
+            R J[W], a[9];
             V3<R> h;
             load_coef(col, S.cf.A, J, a, h);
             const int st = this->col_begin(col), n = this->col_size(col);
-            for (int k = threadIdx.x; k < n; k += NT) {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
-                const V3<R> s = {x[d], y[d], z[d]};
                 const V3<R> hb = gather(col, J, d);
+                const V3<R> s = sp.get(d);
                 const V3<R> as = onsite(a, s);
                 const V3<R> H = {as.x + hb.x - h.x, as.y + hb.y - h.y, as.z + hb.z - h.z};
                 if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
                 const R proj = Math<R>::div_(R(2) * dot(s, H), H.x * H.x + H.y * H.y + H.z * H.z);
-                x[d] = -s.x + proj * H.x;
-                y[d] = -s.y + proj * H.y;
-                z[d] = -s.z + proj * H.z;
+                sp.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
             }
             this->sy.bar();
         }
@@ -453,15 +473,15 @@ template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : Re
     __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
         unsigned acc = 0;
         for (int col = 0; col < S.n_colours; col++) {
-            R J[WMAX], q[9];
+            R J[W], q[9];
             V3<R> h;
             load_coef(col, S.cf.Q, J, q, h);
             const int st = this->col_begin(col), n = this->col_size(col);
-            for (int k = threadIdx.x; k < n; k += NT) {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
                 const uint32_t dg = (uint32_t)this->device_index(col, d);
-                const V3<R> s = {x[d], y[d], z[d]};
                 const V3<R> hb = gather(col, J, d);
+                const V3<R> s = sp.get(d);
                 const V3<R> hext = {hb.x - h.x, hb.y - h.y, hb.z - h.z};
                 const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
@@ -473,9 +493,7 @@ template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : Re
                     accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
                 }
                 if (accept) {
-                    x[d] = sn.x;
-                    y[d] = sn.y;
-                    z[d] = sn.z;
+                    sp.set(d, sn);
                     acc++;
                 }
             }
@@ -487,14 +505,14 @@ template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : Re
     __device__ double energy() const { // valid in thread 0
         double e = 0.0;
         for (int col = 0; col < S.n_colours; col++) {
-            R J[WMAX], m[9];
+            R J[W], m[9];
             V3<R> h;
             load_coef(col, S.cf.E2, J, m, h);
             const int st = this->col_begin(col), n = this->col_size(col);
-            for (int k = threadIdx.x; k < n; k += NT) {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
-                const V3<R> s = {x[d], y[d], z[d]};
                 const V3<R> hb = gather(col, J, d);
+                const V3<R> s = sp.get(d);
                 e += (double)(dot(s, onsite(m, s)) - dot(s, h)) + 0.5 * (double)dot(s, hb);
             }
         }
@@ -505,6 +523,12 @@ template <typename R, int BIL, int ONS, int NT, int CL> struct ResidentFast : Re
 // Probe of iteration q exists?  (q >= t_therm and q % probe_rate == 0)
 __device__ __forceinline__ bool is_probe(const RunDesc &rd, int64_t q) {
     return rd.probe_rate > 0 && q >= rd.t_therm && q % rd.probe_rate == 0;
+}
+
+// Shared memory of one CTA: the spins of its nl local sites, then (specialised
+// kernel, when the lattice's descriptor says so) its nl packed partner words.
+template <typename R> __host__ __device__ constexpr int64_t partner_words_offset(int64_t nl) {
+    return (spin_smem_bytes<R>(nl) + 15) / 16 * 16;
 }
 
 template <typename K, typename R, int NT, int CL>
@@ -532,7 +556,7 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();
     if (CL > 1) cluster_sync_all(); // every rank's phase barrier exists before any remote arrive
     const int64_t dosweep = rd.or_rate == 0 ? 1 : rd.or_rate;
-    const Sync<NT, CL> sync{scratch, red, &pbar, &pphase, cs.error_flag};
+    const Sync<CL> sync{scratch, red, &pbar, &pphase, cs.error_flag};
     int item = CL == 1 ? 0 : (int)cluster_index();
 
     for (;; item += (CL == 1 ? 0 : (int)cluster_count())) {
@@ -547,7 +571,7 @@ __global__ void __launch_bounds__(NT, 1)
             static_assert(sizeof(ResSys<R>) % 4 == 0, "descriptor copied in 4-byte words");
             const uint32_t *src = reinterpret_cast<const uint32_t *>(systems + w.x);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&s_sys);
-            for (int k = threadIdx.x; k < (int)(sizeof(ResSys<R>) / 4); k += NT) dst[k] = src[k];
+            for (int k = threadIdx.x; k < (int)(sizeof(ResSys<R>) / 4); k += blockDim.x) dst[k] = src[k];
         }
         __syncthreads();
         const ResSys<R> &S = s_sys;
@@ -555,31 +579,46 @@ __global__ void __launch_bounds__(NT, 1)
         const int c = S.chain_base + r;
         const int64_t Np = S.tb.Np;
         const int64_t nl = CL == 1 ? Np : S.Npl;
-        R *gx = S.spins + (int64_t)r * 3 * Np;
-        R *x = reinterpret_cast<R *>(smem_raw), *y = x + nl, *z = y + nl;
+        const Spins<R> g = spins_of(S.spins, Np, r); // the replica in device memory
+        const Spins<R> sp = local_spins<R>(smem_raw, nl);
+        const bool words = K::kPartnerWords && S.pv_stage;
+        const uint4 *gwords = CL == 1 ? S.p2v : S.q2v + (int64_t)rank * S.Npl;
+        uint4 *swords = reinterpret_cast<uint4 *>(smem_raw + partner_words_offset<R>(nl));
 
-        // stage this CTA's part of the replica with bulk TMA copies
+        // stage this CTA's part of the replica (and its partner words) with bulk TMA copies
         if (threadIdx.x == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            uint32_t total = words ? (uint32_t)(nl * 16) : 0u;
             if (CL == 1) {
-                const uint32_t bytes = (uint32_t)(Np * sizeof(R));
-                mbar_expect_tx(&bar, 3 * bytes);
-                bulk_g2s(x, gx, bytes, &bar);
-                bulk_g2s(y, gx + Np, bytes, &bar);
-                bulk_g2s(z, gx + 2 * Np, bytes, &bar);
+                total += (uint32_t)spin_smem_bytes<R>(Np);
             } else {
-                uint32_t total = 0;
                 for (int col = 0; col < S.n_colours; col++)
-                    total += 3u * (uint32_t)(((S.loc_count[rank][col] + 31) / 32 * 32) * sizeof(R));
-                mbar_expect_tx(&bar, total);
+                    total += (uint32_t)spin_smem_bytes<R>((S.loc_count[rank][col] + 31) / 32 * 32);
+            }
+            mbar_expect_tx(&bar, total);
+            if (words) bulk_g2s(swords, gwords, (uint32_t)(nl * 16), &bar);
+            if (CL == 1) {
+                if constexpr (sizeof(R) == 4) {
+                    bulk_g2s(sp.p, g.p, (uint32_t)(Np * 16), &bar);
+                } else {
+                    const uint32_t bytes = (uint32_t)(Np * sizeof(R));
+                    bulk_g2s(sp.x, g.x, bytes, &bar);
+                    bulk_g2s(sp.x + Np, g.x + Np, bytes, &bar);
+                    bulk_g2s(sp.x + 2 * Np, g.x + 2 * Np, bytes, &bar);
+                }
+            } else {
                 for (int col = 0; col < S.n_colours; col++) {
                     const int n = (S.loc_count[rank][col] + 31) / 32 * 32;
                     if (n == 0) continue;
-                    const uint32_t bytes = (uint32_t)(n * sizeof(R));
                     const int ls = S.loc_start[rank][col], gs = S.src_start[rank][col];
-                    bulk_g2s(x + ls, gx + gs, bytes, &bar);
-                    bulk_g2s(y + ls, gx + Np + gs, bytes, &bar);
-                    bulk_g2s(z + ls, gx + 2 * Np + gs, bytes, &bar);
+                    if constexpr (sizeof(R) == 4) {
+                        bulk_g2s(sp.p + ls, g.p + gs, (uint32_t)(n * 16), &bar);
+                    } else {
+                        const uint32_t bytes = (uint32_t)(n * sizeof(R));
+                        bulk_g2s(sp.x + ls, g.x + gs, bytes, &bar);
+                        bulk_g2s(sp.x + nl + ls, g.x + Np + gs, bytes, &bar);
+                        bulk_g2s(sp.x + 2 * nl + ls, g.x + 2 * Np + gs, bytes, &bar);
+                    }
                 }
             }
         }
@@ -603,7 +642,7 @@ __global__ void __launch_bounds__(NT, 1)
         }
         if (CL > 1) { // zero this rank's sentinel block, then every rank is staged
             const int sent = S.Npl - 32;
-            for (int k = threadIdx.x; k < 32; k += NT) x[sent + k] = y[sent + k] = z[sent + k] = R(0);
+            for (int k = threadIdx.x; k < 32; k += blockDim.x) sp.set(sent + k, {R(0), R(0), R(0)});
             cluster_sync_all();
         }
 
@@ -611,7 +650,7 @@ __global__ void __launch_bounds__(NT, 1)
         const double T = rd.T_override > 0 ? rd.T_override : cs.T_slot[slot];
         if (threadIdx.x == 0) s_sigma = rd.reset_sigma ? rd.sigma0 : cs.sigma_slot[slot];
         __syncthreads();
-        const K k(S, x, y, z, sync, c, slot, rank, s_coef);
+        const K k(S, sp, sync, c, slot, rank, s_coef, words ? swords : gwords);
         k.prepare();
         const R invT = (R)(1.0 / T);
         const bool writer = threadIdx.x == 0 && rank == 0;
@@ -623,19 +662,6 @@ __global__ void __launch_bounds__(NT, 1)
         uint64_t sweeps = rd.sweeps0;
         const uint64_t every = rd.renorm_every > 0 ? (uint64_t)rd.renorm_every : 0;
         uint64_t next_renorm = every ? (sweeps / every + 1) * every : 0;
-
-        if (rd.pending_probe) { // probe of the exchange iteration it0-1
-            const int64_t q = rd.it0 - 1;
-            const double M = k.magnetization();
-            if (writer) {
-                const int64_t kq = (q - rd.probe_first) / rd.probe_rate;
-                if (kq >= 0 && kq < rd.probe_cap) {
-                    if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
-                    if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
-                }
-                cs.M_chain[c] = M;
-            }
-        }
 
         for (int64_t it = rd.it0; it < rd.it1; it++) {
             if (rd.or_rate != 0) {
@@ -668,12 +694,14 @@ __global__ void __launch_bounds__(NT, 1)
                     if (threadIdx.x == 0) E = e;
                 }
             }
+            // a probe at an exchange iteration (the window's last) is recorded
+            // by the exchange kernel after the exchange, from M_chain
             const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-            if (is_probe(rd, it) && !swap_here) {
+            if (is_probe(rd, it)) {
                 const double M = k.magnetization();
                 if (writer) {
                     const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
-                    if (kq >= 0 && kq < rd.probe_cap) {
+                    if (!swap_here && kq >= 0 && kq < rd.probe_cap) {
                         if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
                         if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
                     }
@@ -691,26 +719,64 @@ __global__ void __launch_bounds__(NT, 1)
             cs.acc_slot[slot] += acc_total;
             cs.sigma_slot[slot] = s_sigma;
         }
+        // every thread's shared-memory accesses are ordered before the bulk
+        // copies that follow (the stores below, the next item's staging)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        // write this CTA's part back (x, y, z are contiguous in both memories)
-        if (CL == 1) {
-            for (int64_t i = threadIdx.x; i < 3 * Np; i += NT) gx[i] = x[i];
+        // write this CTA's part back: bulk TMA stores of the float4 sites
+        // (single precision), a store loop over the component blocks (double)
+        if constexpr (sizeof(R) == 4) {
+            if (threadIdx.x == 0) {
+                if (CL == 1) {
+                    bulk_s2g(g.p, sp.p, (uint32_t)(Np * 16));
+                } else {
+                    for (int col = 0; col < S.n_colours; col++) {
+                        const int n = S.loc_count[rank][col];
+                        if (n > 0) bulk_s2g(g.p + S.src_start[rank][col], sp.p + S.loc_start[rank][col], (uint32_t)(n * 16));
+                    }
+                }
+                bulk_commit_and_wait();
+            }
         } else {
-            for (int col = 0; col < S.n_colours; col++) {
-                const int n = S.loc_count[rank][col], ls = S.loc_start[rank][col], gs = S.src_start[rank][col];
-                for (int i = threadIdx.x; i < n; i += NT) {
-                    gx[gs + i] = x[ls + i];
-                    gx[Np + gs + i] = y[ls + i];
-                    gx[2 * Np + gs + i] = z[ls + i];
+            if (CL == 1) {
+                for (int64_t i = threadIdx.x; i < 3 * Np; i += blockDim.x) g.x[i] = sp.x[i];
+            } else {
+                for (int col = 0; col < S.n_colours; col++) {
+                    const int n = S.loc_count[rank][col], ls = S.loc_start[rank][col], gs = S.src_start[rank][col];
+                    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                        g.x[gs + i] = sp.x[ls + i];
+                        g.x[Np + gs + i] = sp.x[nl + ls + i];
+                        g.x[2 * Np + gs + i] = sp.x[2 * nl + ls + i];
+                    }
                 }
             }
-            cluster_sync_all(); // no rank reads another's shared memory past this point
         }
+        if (CL > 1) cluster_sync_all(); // no rank reads another's shared memory past this point
         __syncthreads();
     }
 }
 
 // Kernel entry points of each instantiation family (resident_*.cu).
-template <typename R> const void *resident_kernel_generic(int block, bool cub, bool qua);
+template <typename R> const void *resident_kernel_generic(bool cub, bool qua);
+// specialised kernels of width W (defined in resident_fast_<precision>_w<W>.cu)
+template <typename R, int W> const void *resident_kernel_fast(int bil, int ons, int cl);
+
+template <typename R, int W, int BIL, int ONS, int CL> const void *resident_fast_kernel() {
+    using K = ResidentFast<R, BIL, ONS, W, CL>;
+    static_assert(K::kMaxThreads == resident_max_threads(true, BIL, ONS), "launch bound");
+    return (const void *)k_resident<K, R, K::kMaxThreads, CL>;
+}
+template <typename R, int W, int BIL, int ONS> const void *resident_fast_for(int cl) {
+    if (cl == 4) return resident_fast_kernel<R, W, BIL, ONS, 4>();
+    if (cl == 2) return resident_fast_kernel<R, W, BIL, ONS, 2>();
+    return resident_fast_kernel<R, W, BIL, ONS, 1>();
+}
+template <typename R, int W> const void *resident_fast_table(int bil, int ons, int cl) {
+    if (bil == 0)
+        return ons == 0 ? resident_fast_for<R, W, 0, 0>(cl)
+                        : ons == 1 ? resident_fast_for<R, W, 0, 1>(cl) : resident_fast_for<R, W, 0, 2>(cl);
+    return ons == 0 ? resident_fast_for<R, W, 1, 0>(cl)
+                    : ons == 1 ? resident_fast_for<R, W, 1, 1>(cl) : resident_fast_for<R, W, 1, 2>(cl);
+}
 
 } // namespace csmc

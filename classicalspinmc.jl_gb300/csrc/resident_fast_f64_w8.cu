@@ -1,0 +1,13 @@
+// resident_fast_f64_w8.cu -- instantiations of the specialised resident kernel (resident.cuh)
+// in double precision for 8 bilinear partners per site: every bilinear class
+// (scalar / general 3x3), onsite class (none / diagonal / general) and cluster
+// size (1, 2 or 4 CTAs per replica).
+#include "resident.cuh"
+
+namespace csmc {
+
+template <> const void *resident_kernel_fast<double, 8>(int bil, int ons, int cl) {
+    return resident_fast_table<double, 8>(bil, ons, cl);
+}
+
+} // namespace csmc

@@ -5,24 +5,19 @@
 
 namespace csmc {
 
-template <typename R, int NT> static const void *generic_for(bool cub, bool qua) {
-    if (cub && qua) return (const void *)k_resident<ResidentGeneric<R, true, true, NT, 1>, R, NT, 1>;
-    if (cub) return (const void *)k_resident<ResidentGeneric<R, true, false, NT, 1>, R, NT, 1>;
-    if (qua) return (const void *)k_resident<ResidentGeneric<R, false, true, NT, 1>, R, NT, 1>;
-    return (const void *)k_resident<ResidentGeneric<R, false, false, NT, 1>, R, NT, 1>;
+template <typename R> const void *resident_kernel_generic(bool cub, bool qua) {
+    constexpr int NT = resident_max_threads(false, 0, 0);
+    if (cub && qua) return (const void *)k_resident<ResidentGeneric<R, true, true, 1>, R, NT, 1>;
+    if (cub) return (const void *)k_resident<ResidentGeneric<R, true, false, 1>, R, NT, 1>;
+    if (qua) return (const void *)k_resident<ResidentGeneric<R, false, true, 1>, R, NT, 1>;
+    return (const void *)k_resident<ResidentGeneric<R, false, false, 1>, R, NT, 1>;
 }
 
-template <typename R> const void *resident_kernel_generic(int block, bool cub, bool qua) {
-    return block == 1024 ? generic_for<R, 1024>(cub, qua) : generic_for<R, 512>(cub, qua);
-}
-
-const void *resident_kernel_fast_f32(int block, int bil, int ons, int cl);
-const void *resident_kernel_fast_f64(int block, int bil, int ons, int cl);
-
-template <typename R> static const void *pick(int block, const ResidentSel &sel) {
-    if (!sel.fast) return resident_kernel_generic<R>(block, sel.cub, sel.qua);
-    return sizeof(R) == 4 ? resident_kernel_fast_f32(block, sel.bil, sel.ons, sel.cl)
-                          : resident_kernel_fast_f64(block, sel.bil, sel.ons, sel.cl);
+template <typename R> static const void *pick(const ResidentSel &sel) {
+    if (!sel.fast) return resident_kernel_generic<R>(sel.cub, sel.qua);
+    if (sel.width <= 4) return resident_kernel_fast<R, 4>(sel.bil, sel.ons, sel.cl);
+    if (sel.width <= 6) return resident_kernel_fast<R, 6>(sel.bil, sel.ons, sel.cl);
+    return resident_kernel_fast<R, 8>(sel.bil, sel.ons, sel.cl);
 }
 
 template <typename R>
@@ -30,7 +25,9 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
                             const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem,
                             const ResidentSel &sel, cudaStream_t st) {
     // work_ctr must be zero when the kernel starts (the caller resets it on `st`)
-    const void *fn = pick<R>(block, sel);
+    if (block < 32 || block > resident_max_threads(sel.fast, sel.bil, sel.ons) || block % 32 != 0)
+        return cudaErrorInvalidValue;
+    const void *fn = pick<R>(sel);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     ChainState csv = cs;
@@ -54,7 +51,7 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
 
 // Resident CTAs (cl = 1) or clusters (cl > 1) that fit on the device at once.
 template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms) {
-    const void *fn = pick<R>(block, sel);
+    const void *fn = pick<R>(sel);
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
     if (sel.cl <= 1) {
         int n = 0;
@@ -77,13 +74,23 @@ template <typename R> int resident_capacity(int block, size_t smem, const Reside
     return n;
 }
 
-template const void *resident_kernel_generic<float>(int, bool, bool);
-template const void *resident_kernel_generic<double>(int, bool, bool);
+// Static shared memory of the selected kernel (its descriptor copy, reduction
+// scratch and staged couplings), or -1.
+template <typename R> int resident_static_smem(const ResidentSel &sel) {
+    cudaFuncAttributes at{};
+    if (cudaFuncGetAttributes(&at, pick<R>(sel)) != cudaSuccess) return -1;
+    return (int)at.sharedSizeBytes;
+}
+
+template const void *resident_kernel_generic<float>(bool, bool);
+template const void *resident_kernel_generic<double>(bool, bool);
 template cudaError_t launch_resident<float>(const ResSys<float> *, const int2 *, int, int *, const ChainState &,
                                             const RunDesc &, int, int, size_t, const ResidentSel &, cudaStream_t);
 template cudaError_t launch_resident<double>(const ResSys<double> *, const int2 *, int, int *, const ChainState &,
                                              const RunDesc &, int, int, size_t, const ResidentSel &, cudaStream_t);
 template int resident_capacity<float>(int, size_t, const ResidentSel &, int);
 template int resident_capacity<double>(int, size_t, const ResidentSel &, int);
+template int resident_static_smem<float>(const ResidentSel &);
+template int resident_static_smem<double>(const ResidentSel &);
 
 } // namespace csmc
