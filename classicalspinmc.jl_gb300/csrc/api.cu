@@ -76,7 +76,6 @@ struct System {
     std::vector<int32_t> col_pattern;
     // split over a thread-block cluster (context-wide cluster size > 1)
     ClusterLayout cl_layout;
-    DevBuf<uint16_t> q2c;
     // bilinear partners packed 8 x 16 bit per site (specialised kernel)
     DevBuf<uint4> p2v, q2v;
     size_t resident_smem = 0;
@@ -357,7 +356,6 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     const ClusterLayout &L = S.cl_layout;
     r.cl = L.ranks;
     r.Npl = (int32_t)L.Npl;
-    r.q2c = S.q2c.p;
     r.p2v = S.p2v.p;
     r.q2v = S.q2v.p;
     r.pv_stage = S.pv_stage ? 1 : 0;
@@ -423,7 +421,6 @@ static void choose_cluster(Ctx &C, int requested) {
         System &S = *Sp;
         if (best > 1) {
             S.cl_layout = make_cluster_layout(S.plan, best);
-            S.q2c.upload(S.cl_layout.q2);
             {
                 const ClusterLayout &L = S.cl_layout;
                 const int W = std::max(S.plan.W2, 1);
@@ -431,7 +428,7 @@ static void choose_cluster(Ctx &C, int requested) {
                 for (int k = 0; k < L.ranks; k++) {
                     std::vector<uint16_t> part(L.q2.begin() + (size_t)k * W * L.Npl,
                                                L.q2.begin() + (size_t)(k + 1) * W * L.Npl);
-                    const uint32_t sent = (uint32_t)((k << 14) | (L.Npl - 32));
+                    const uint32_t sent = (uint32_t)(L.Npl - 32);
                     std::vector<uint4> pk = pack8(part, S.plan.W2, L.Npl, [&](int64_t) { return sent; });
                     all.insert(all.end(), pk.begin(), pk.end());
                 }

@@ -50,14 +50,15 @@ template <typename R> struct ResSys {
     R S;
     uint32_t k0, k1;
     // split over a cluster of `cl` CTAs (cl > 1): per rank and colour class,
-    // the local start, the site count and the device index of the first site;
-    // partners q2c[rank][W2][Npl] encoded (owner rank << 14) | owner-local index
+    // the local start, the site count and the device index of the first site
     int32_t cl, Npl;
     int32_t loc_start[4][CSMC_MAX_COLOURS], loc_count[4][CSMC_MAX_COLOURS], src_start[4][CSMC_MAX_COLOURS];
-    const uint16_t *q2c;
     // the bilinear partners of each site packed in one 16-byte word (up to 8
-    // 16-bit partners, sentinel-padded): p2v[i] for one CTA per replica,
-    // q2v[rank][i] for clusters; used by the specialised kernel
+    // 16-bit partners, sentinel-padded): p2v[i] (device index) for one CTA
+    // per replica; q2v[rank][i] for clusters, each entry
+    // (owner rank - rank mod cl) << 14 | owner-local index, so partners in the
+    // reading CTA's own shared memory have the top two bits clear; used by
+    // the specialised kernel
     const uint4 *p2v, *q2v;
     // nonzero: the specialised kernel stages the CTA's partner words in
     // shared memory too (they fit beside the spins)
@@ -82,7 +83,7 @@ constexpr int RESIDENT_WMAX = 8; // bilinear slots per site of the specialised k
 // the specialised kernel with scalar couplings and at most diagonal onsite
 // terms (64 registers per thread suffice), else 512.
 __host__ __device__ constexpr int resident_max_threads(bool fast, int bil, int ons) {
-    return fast && bil == 0 && ons < 2 ? 1024 : 512;
+    return fast && bil == 0 && ons < 2 ? 896 : 512;
 }
 
 // The sweep schedule of one resident launch (see csmc_run_params).

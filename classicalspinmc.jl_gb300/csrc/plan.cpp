@@ -706,21 +706,23 @@ ClusterLayout make_cluster_layout(const Plan &P, int ranks) {
     L.Npl = mx + 32; // sentinel block at local index mx
     require(L.Npl <= 16384, CSMC_ERR_UNSUPPORTED, "a cluster rank would hold more than 16383 sites");
     const int64_t sent_local = mx;
-    // device index -> (owner, local)
+    // device index -> (owner relative to the reader, owner-local index); the
+    // reader's own sites and the sentinel have relative owner 0
     auto locate = [&](int64_t d, int reader) -> uint16_t {
-        if (d == P.sentinel || d < 0) return (uint16_t)((reader << 14) | sent_local);
+        if (d == P.sentinel || d < 0) return (uint16_t)sent_local;
         int c = 0;
         while (c + 1 < C && d >= P.col_start[c + 1]) c++;
         const int64_t off = d - P.col_start[c];
         const int k = (int)(off / L.part[c]);
         const int64_t local = L.loc_start[k * C + c] + (off - k * L.part[c]);
-        return (uint16_t)((k << 14) | local);
+        const int rel = (k - reader + ranks) % ranks;
+        return (uint16_t)((rel << 14) | local);
     };
     const int W = std::max(P.W2, 1);
     L.q2.assign((size_t)ranks * W * L.Npl, 0);
     for (int k = 0; k < ranks; k++) {
         for (int t = 0; t < W; t++)
-            for (int64_t i = 0; i < L.Npl; i++) L.q2[((size_t)k * W + t) * L.Npl + i] = (uint16_t)((k << 14) | sent_local);
+            for (int64_t i = 0; i < L.Npl; i++) L.q2[((size_t)k * W + t) * L.Npl + i] = (uint16_t)sent_local;
         for (int c = 0; c < C; c++)
             for (int64_t j = 0; j < L.loc_count[k * C + c]; j++) {
                 const int64_t d = L.src_start[k * C + c] + j, i = L.loc_start[k * C + c] + j;

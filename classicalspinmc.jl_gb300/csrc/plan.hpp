@@ -94,7 +94,8 @@ struct ClusterLayout {
     std::vector<int64_t> loc_start;      // [rank][colour]
     std::vector<int64_t> loc_count;      // [rank][colour]
     std::vector<int64_t> src_start;      // [rank][colour] device index of the part's first site
-    std::vector<uint16_t> q2;            // [rank][W2][Npl]
+    // [rank][W2][Npl]: (owner rank - reading rank mod ranks) << 14 | owner-local index
+    std::vector<uint16_t> q2;
 };
 // Throws csmc::Error if a rank would hold more than 16383 sites.
 ClusterLayout make_cluster_layout(const Plan &p, int ranks);

@@ -354,7 +354,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     static_assert(W == 4 || W == 6 || W == 8, "partner widths 4, 6 and 8");
     // scalar couplings and at most diagonal onsite terms fit 64 registers per
     // thread (1024 threads); 3x3 couplings or general onsite terms get 128
-    static constexpr int kMaxThreads = (BIL == 0 && ONS < 2) ? 1024 : 512;
+    static constexpr int kMaxThreads = (BIL == 0 && ONS < 2) ? 896 : 512;
     static constexpr int WMAX = RESIDENT_WMAX;
     static constexpr int kCoefSmem = BIL ? CSMC_MAX_COLOURS * WMAX * 9 : 1;
     static constexpr bool kPartnerWords = true;
@@ -365,7 +365,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     using B::scoef;
     using B::sp;
     const uint4 *pv; // packed partner words of this CTA's sites, by local index (shared or global memory)
-    uint32_t rb[CL]; // shared::cluster address of local site 0 in every rank (CL > 1)
+    uint32_t rb[CL]; // shared::cluster address of local site 0 of rank (rank + q) % CL, by q (CL > 1)
     uint32_t comp;   // double precision: bytes between the x, y and z blocks
 
     __device__ ResidentFast(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
@@ -375,7 +375,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         if (CL > 1) {
             const uint32_t a = smem_u32(spin_base(sp));
 #pragma unroll
-            for (int r = 0; r < CL; r++) rb[r] = map_rank(a, r);
+            for (int q = 0; q < CL; q++) rb[q] = map_rank(a, (uint32_t)((rk + q) % CL));
         }
     }
 
@@ -423,27 +423,35 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         }
     }
 
-    // the spin of partner entry v: a local index (CL = 1) or
-    // (owner rank << 14) | owner-local index (CL > 1)
-    __device__ __forceinline__ V3<R> partner(uint32_t v) const {
-        if (CL == 1) return sp.get((int)v);
-        const uint32_t owner = v >> 14, local = v & 0x3FFFu;
+    // the spin of cluster partner entry v = (relative owner q << 14) |
+    // owner-local index, read through the shared::cluster window
+    __device__ __forceinline__ V3<R> partner_cluster(uint32_t v) const {
+        const uint32_t q = v >> 14, local = v & 0x3FFFu;
         uint32_t b = rb[0];
-        if (CL == 2) b = owner ? rb[1 % CL] : rb[0];
-        if (CL == 4)
-            b = (owner & 2u) ? ((owner & 1u) ? rb[3 % CL] : rb[2 % CL]) : ((owner & 1u) ? rb[1 % CL] : rb[0]);
+        if (CL == 2) b = q ? rb[1 % CL] : rb[0];
+        if (CL == 4) b = (q & 2u) ? ((q & 1u) ? rb[3 % CL] : rb[2 % CL]) : ((q & 1u) ? rb[1 % CL] : rb[0]);
         return cluster_spin(b + local * site_stride<R>(), comp, R(0));
     }
 
     // sum over bilinear slots of J_t s_j at local site i: the partner entries
-    // come in one 16-byte word, every partner load is issued before use
+    // come in one 16-byte word, every partner load is issued before use.  In
+    // a cluster, a warp whose sites all have their partners in this CTA reads
+    // them with plain shared-memory loads; a warp with any partner in another
+    // rank reads all of its partners through the cluster window.
     __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], int i) const {
         const uint4 w = pv[i];
         const uint32_t v[8] = {w.x & 0xFFFFu, w.x >> 16, w.y & 0xFFFFu, w.y >> 16,
                                w.z & 0xFFFFu, w.z >> 16, w.w & 0xFFFFu, w.w >> 16};
         V3<R> s[W];
+        bool local = true;
+        if (CL > 1) local = !__any_sync(__activemask(), ((w.x | w.y | w.z | w.w) & 0xC000C000u) != 0u);
+        if (local) {
 #pragma unroll
-        for (int t = 0; t < W; t++) s[t] = partner(v[t]);
+            for (int t = 0; t < W; t++) s[t] = sp.get((int)v[t]);
+        } else {
+#pragma unroll
+            for (int t = 0; t < W; t++) s[t] = partner_cluster(v[t]);
+        }
         V3<R> hb = {R(0), R(0), R(0)};
 #pragma unroll
         for (int t = 0; t < W; t++) accumulate(hb, col, t, J, s[t]);
