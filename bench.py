@@ -152,8 +152,17 @@ def bench_ours(args, rank, world, dist):
     ctx = m.monte_carlo.Context([lat], [R_REPL], precision="fp32", seed=SEED + rank)
     ctx.set_temperatures(temperatures())
     ctx.call("csmc_random_spins", C.c_uint64(SEED + 1000 * rank))
+    tuned = []
     if args.cluster:
         ctx.call("csmc_set_cluster_size", args.cluster)
+    elif not args.no_autotune and not args.block:
+        # the library's autotuner picks CTAs per replica and threads per CTA on
+        # these replicas (state restored exactly afterwards)
+        entries = (L.TuneEntry * 8)()
+        n = C.c_int32()
+        ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 8, C.byref(n))
+        tuned = [{"cluster": e.cluster, "block": e.block, "ms_per_window": round(e.ms_per_window, 5),
+                  "chosen": bool(e.chosen)} for e in entries[:n.value]]
     ranks = C.c_int32()
     ctx.call("csmc_cluster_size", C.byref(ranks))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -192,7 +201,7 @@ def bench_ours(args, rank, world, dist):
         t_dev = float(tt.item())
     value = world * upd * args.steps / t_dev
     out = {"value": value, "ms_per_step": 1e3 * t_dev / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
-           "gpu_launches": launches, "clocks": clk.summary(), "ctas_per_replica": ranks.value}
+           "gpu_launches": launches, "clocks": clk.summary(), "ctas_per_replica": ranks.value, "autotune": tuned}
     # roofline of the dominant kernel (the resident sweep kernel, one launch per step)
     per_launch_s = kern_ms / 1e3 / max(kern_launches, 1)
     bytes_per_launch = upd * BYTES_PER_UPDATE_FP32 * args.steps / max(kern_launches, 1)
@@ -381,7 +390,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
-    ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: library default; 1, 2 or 4)")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: autotuned; 1, 2 or 4)")
+    ap.add_argument("--no-autotune", action="store_true", help="skip csmc_autotune (library heuristics)")
     ap.add_argument("--workload", default="sc_pt",
                     choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
                              "pyrochlore_large_fp32"],
@@ -429,7 +439,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config({"precision": "FP32 spins/fields/dE, FP64 energies+exchange+observables",
                                        "wall_ms_per_step": res["wall_ms_per_step"],
-                                       "ctas_per_replica": res["ctas_per_replica"]}),
+                                       "ctas_per_replica": res["ctas_per_replica"],
+                                       "autotune_candidates": res["autotune"]}),
             "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "clocks": res["clocks"],
             "gpu_launches": res["gpu_launches"]}
     if "plain_fp64_per_replica" in res:

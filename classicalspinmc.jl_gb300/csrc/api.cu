@@ -104,7 +104,8 @@ struct Ctx {
     DevBuf<int2> items;
     DevBuf<int2> lattices; // per lattice {first slot, replicas} (exchange kernel)
     int n_items = 0;
-    int cl = 1; // CTAs per replica of the resident kernel
+    int cl = 1;         // CTAs per replica of the resident kernel
+    int block_pref = 0; // threads per CTA chosen by csmc_autotune (0: automatic)
     uint32_t msweep = 0;   // Metropolis sweeps so far (the Philox counter)
     uint64_t nsweeps = 0;  // sweeps of every kind so far (renormalisation cadence)
     int renorm_every = 64;
@@ -784,6 +785,7 @@ static int choose_path(Ctx &C, int requested) {
 static int resident_block(Ctx &C, int hint) {
     const ResidentSel sel = resident_selection(C);
     const int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
+    if (hint == 0 && C.block_pref > 0) hint = C.block_pref;
     if (hint > 0) {
         require(hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
         return std::min(hint, mx);
@@ -1485,6 +1487,128 @@ int csmc_cluster_size(void *c, int32_t *ranks) {
     API_BEGIN
     require(ranks != nullptr, CSMC_ERR_INVALID, "ranks is NULL");
     *ranks = ctx_of(c).cl;
+    API_END
+}
+
+// ------------------------------------------------------------ autotuner
+
+namespace csmc {
+
+// Device state a run changes, copied aside and back so that timing runs leave
+// the chain exactly where it was.
+struct StateCopy {
+    std::vector<std::pair<void *, size_t>> parts;
+    DevBuf<unsigned char> buf;
+    uint32_t msweep = 0;
+    uint64_t nsweeps = 0;
+    explicit StateCopy(Ctx &C) {
+        for (auto &S : C.sys) {
+            if (C.precision == CSMC_FP32) parts.push_back({S->fspins.p, S->fspins.n * sizeof(float)});
+            else parts.push_back({S->dspins.p, S->dspins.n * sizeof(double)});
+        }
+        parts.push_back({C.slot_of.p, C.slot_of.n * sizeof(int32_t)});
+        parts.push_back({C.chain_of.p, C.chain_of.n * sizeof(int32_t)});
+        for (DevBuf<double> *b : {&C.sigma_slot, &C.acc_slot, &C.exch_slot, &C.E_chain, &C.M_chain, &C.last_acc})
+            parts.push_back({b->p, b->n * sizeof(double)});
+        parts.push_back({C.sweep_acc.p, C.sweep_acc.n * sizeof(unsigned long long)});
+        size_t total = 0;
+        for (auto &q : parts) total += (q.second + 255) / 256 * 256;
+        buf.alloc(total);
+        copy(C, true);
+        msweep = C.msweep;
+        nsweeps = C.nsweeps;
+    }
+    void copy(Ctx &C, bool save) {
+        size_t off = 0;
+        for (auto &q : parts) {
+            void *a = buf.p + off;
+            CK(cudaMemcpyAsync(save ? a : q.first, save ? q.first : a, q.second, cudaMemcpyDeviceToDevice, C.st));
+            off += (q.second + 255) / 256 * 256;
+        }
+    }
+    void restore(Ctx &C) {
+        copy(C, false);
+        C.msweep = msweep;
+        C.nsweeps = nsweeps;
+        CK(cudaStreamSynchronize(C.st));
+    }
+};
+
+// Time the resident kernel's launch configurations on the context's own
+// replicas: every cluster size that fits (1, 2, 4) with the balanced block
+// size and with the kernel's largest block; keep the fastest.
+static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_entry *out, int capacity,
+                     int *n_out) {
+    require(p != nullptr && n_windows >= 1, CSMC_ERR_INVALID, "autotune needs run parameters and n_windows >= 1");
+    *n_out = 0;
+    if (choose_path(C, p->path) != CSMC_PATH_RESIDENT) return; // nothing to tune: the run takes the global path
+    csmc_run_params q = *p;
+    q.path = CSMC_PATH_RESIDENT;
+    q.resident_block = 0;
+    q.probe_energy = q.probe_magnetization = nullptr;
+    q.probe_capacity = 0;
+    q.accepted = q.exchanged = nullptr;
+    const int span = q.swap_rate > 0 ? q.swap_rate : std::max(q.overrelaxation_rate, 1) * 10;
+    q.n_sweeps = (int64_t)n_windows * span;
+    const int cl0 = C.cl, bp0 = C.block_pref;
+    StateCopy saved(C);
+    struct Cand {
+        int cl, block;
+        double ms;
+    };
+    std::vector<Cand> cands;
+    for (int cl : {1, 2, 4}) {
+        try {
+            choose_cluster(C, cl);
+        } catch (const Error &) {
+            continue; // this size does not apply to these lattices
+        }
+        bool ok = true;
+        for (auto &S : C.sys) ok = ok && S->resident_ok;
+        if (!ok) continue;
+        upload_resident(C);
+        C.block_pref = 0;
+        const ResidentSel sel = resident_selection(C);
+        const int balanced = resident_block(C, 0), largest = resident_max_threads(sel.fast, sel.bil, sel.ons);
+        for (int block : {balanced, largest}) {
+            if (block == largest && largest == balanced && !cands.empty() && cands.back().cl == cl) continue;
+            C.block_pref = block;
+            run(C, &q); // warm-up (first launch of this kernel)
+            saved.restore(C);
+            run(C, &q);
+            cands.push_back({cl, block, C.last_ms / n_windows});
+            saved.restore(C);
+        }
+    }
+    require(!cands.empty(), CSMC_ERR_UNSUPPORTED, "no resident configuration fits these lattices");
+    size_t best = 0;
+    for (size_t k = 1; k < cands.size(); k++)
+        if (cands[k].ms < cands[best].ms) best = k;
+    (void)cl0;
+    (void)bp0;
+    choose_cluster(C, cands[best].cl);
+    upload_resident(C);
+    C.block_pref = cands[best].block;
+    for (size_t k = 0; k < cands.size() && (int)k < capacity; k++) {
+        out[k].cluster = cands[k].cl;
+        out[k].block = cands[k].block;
+        out[k].ms_per_window = cands[k].ms;
+        out[k].chosen = k == best ? 1 : 0;
+    }
+    *n_out = (int)cands.size();
+}
+
+} // namespace csmc
+
+int csmc_autotune(void *c, const csmc_run_params *params, int32_t n_windows, csmc_tune_entry *entries,
+                  int32_t capacity, int32_t *n_entries) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(n_entries != nullptr && (capacity == 0 || entries != nullptr), CSMC_ERR_INVALID, "entries missing");
+    int n = 0;
+    CK(cudaStreamSynchronize(C.st));
+    autotune(C, params, n_windows, entries, capacity, &n);
+    *n_entries = n;
     API_END
 }
 

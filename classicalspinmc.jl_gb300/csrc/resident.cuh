@@ -288,7 +288,7 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
     using B::S;
     using B::sp;
     __device__ ResidentGeneric(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
-                               const uint4 *)
+                               const uint4 *, bool)
         : B{s, sp_, sy_, c_, slot_, rk, coef} {}
     __device__ void prepare() const {}
 
@@ -356,7 +356,11 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     // thread (1024 threads); 3x3 couplings or general onsite terms get 128
     static constexpr int kMaxThreads = (BIL == 0 && ONS < 2) ? 896 : 512;
     static constexpr int WMAX = RESIDENT_WMAX;
-    static constexpr int kCoefSmem = BIL ? CSMC_MAX_COLOURS * WMAX * 9 : 1;
+    // per colour class in shared memory: J[W], A[9], Q[9], E2[9], h[3]; then
+    // (3x3 couplings) the matrices [colour][W][9]
+    static constexpr int kClassBlock = WMAX + 30;
+    static constexpr int kCoefSmem = CSMC_MAX_COLOURS * kClassBlock + (BIL ? CSMC_MAX_COLOURS * WMAX * 9 : 0);
+    static constexpr int OFF_A = WMAX, OFF_Q = WMAX + 9, OFF_E2 = WMAX + 18, OFF_H = WMAX + 27;
     static constexpr bool kPartnerWords = true;
     using B = ResidentCommon<R, CL>;
     using B::c;
@@ -365,12 +369,14 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     using B::scoef;
     using B::sp;
     const uint4 *pv; // packed partner words of this CTA's sites, by local index (shared or global memory)
+    uint32_t pvs;    // their shared-memory address when staged there, else 0
     uint32_t rb[CL]; // shared::cluster address of local site 0 of rank (rank + q) % CL, by q (CL > 1)
     uint32_t comp;   // double precision: bytes between the x, y and z blocks
 
     __device__ ResidentFast(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
-                            const uint4 *pv_)
+                            const uint4 *pv_, bool pv_shared)
         : B{s, sp_, sy_, c_, slot_, rk, coef}, pv(pv_) {
+        pvs = pv_shared ? smem_u32(pv_) : 0u;
         comp = (uint32_t)(S.Npl * sizeof(double));
         if (CL > 1) {
             const uint32_t a = smem_u32(spin_base(sp));
@@ -379,29 +385,41 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         }
     }
 
-    // stage the 3x3 couplings of every colour class, zero for slots beyond
-    // the lattice's W2: scoef[(col*W + t)*9 + e]
+    // stage the couplings of every colour class in shared memory (slots
+    // beyond the lattice's W2 are zero): the class blocks, and the 3x3
+    // matrices at scoef[MAX_COLOURS * kClassBlock + (col*W + t)*9 + e]
     __device__ void prepare() const {
+        const int W2 = S.tb.W2;
+        for (int k = threadIdx.x; k < S.n_colours * kClassBlock; k += blockDim.x) {
+            const int col = k / kClassBlock, e = k - col * kClassBlock, b = S.col_pattern[col];
+            R v = R(0);
+            if (e < WMAX) v = (BIL == 0 && e < W2) ? S.cf.Js[b * W2 + e] : R(0);
+            else if (e < OFF_Q) v = S.cf.A[9 * b + e - OFF_A];
+            else if (e < OFF_E2) v = S.cf.Q[9 * b + e - OFF_Q];
+            else if (e < OFF_H) v = S.cf.E2[9 * b + e - OFF_E2];
+            else v = S.cf.h[3 * b + e - OFF_H];
+            scoef[k] = v;
+        }
         if (BIL) {
-            const int W2 = S.tb.W2, n = S.n_colours * W * 9;
+            const int n = S.n_colours * W * 9;
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int col = k / (W * 9), rem = k - col * W * 9, t = rem / 9, e = rem - t * 9;
                 const int b = S.col_pattern[col];
-                scoef[k] = t < W2 ? S.cf.mats[9 * S.cf.c2[b * W2 + t] + e] : R(0);
+                scoef[CSMC_MAX_COLOURS * kClassBlock + k] = t < W2 ? S.cf.mats[9 * S.cf.c2[b * W2 + t] + e] : R(0);
             }
-            __syncthreads();
         }
+        __syncthreads();
     }
 
-    // per colour class: slot scalars J (zero beyond the lattice's W2), an
-    // onsite-class matrix m (from A, Q or E2) and the field h
-    __device__ __forceinline__ void load_coef(int col, const R *src, R (&J)[W], R (&m)[9], V3<R> &h) const {
-        const int b = S.col_pattern[col], W2 = S.tb.W2;
+    // per colour class, from shared memory: slot scalars J, the onsite-class
+    // matrix m at offset `which` (OFF_A, OFF_Q or OFF_E2) and the field h
+    __device__ __forceinline__ void load_coef(int col, int which, R (&J)[W], R (&m)[9], V3<R> &h) const {
+        const R *blk = scoef + col * kClassBlock;
 #pragma unroll
-        for (int t = 0; t < W; t++) J[t] = (BIL == 0 && t < W2) ? S.cf.Js[b * W2 + t] : R(0);
+        for (int t = 0; t < W; t++) J[t] = BIL == 0 ? blk[t] : R(0);
 #pragma unroll
-        for (int k = 0; k < 9; k++) m[k] = ONS == 0 ? R(0) : src[9 * b + k];
-        h = {S.cf.h[3 * b], S.cf.h[3 * b + 1], S.cf.h[3 * b + 2]};
+        for (int k = 0; k < 9; k++) m[k] = ONS == 0 ? R(0) : blk[which + k];
+        h = {blk[OFF_H], blk[OFF_H + 1], blk[OFF_H + 2]};
     }
 
     __device__ __forceinline__ V3<R> onsite(const R (&m)[9], V3<R> s) const {
@@ -416,7 +434,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
             hb.y += J[t] * s.y;
             hb.z += J[t] * s.z;
         } else {
-            const R *M = scoef + (col * W + t) * 9;
+            const R *M = scoef + CSMC_MAX_COLOURS * kClassBlock + (col * W + t) * 9;
             hb.x += M[0] * s.x + M[1] * s.y + M[2] * s.z;
             hb.y += M[3] * s.x + M[4] * s.y + M[5] * s.z;
             hb.z += M[6] * s.x + M[7] * s.y + M[8] * s.z;
@@ -438,8 +456,26 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     // a cluster, a warp whose sites all have their partners in this CTA reads
     // them with plain shared-memory loads; a warp with any partner in another
     // rank reads all of its partners through the cluster window.
-    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], int i) const {
-        const uint4 w = pv[i];
+    __device__ __forceinline__ uint4 word(int i) const {
+        uint4 w;
+        if (pvs) // block-uniform
+            asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(w.x), "=r"(w.y), "=r"(w.z), "=r"(w.w)
+                         : "r"(pvs + 16u * (uint32_t)i));
+        else
+            w = pv[i];
+        return w;
+    }
+    // the partner word of the first site of this thread in [st, st + n)
+    __device__ __forceinline__ uint4 first_word(int st, int n) const {
+        return (int)threadIdx.x < n ? word(st + (int)threadIdx.x) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    // the partner word of the next site of this thread (loaded one site ahead)
+    __device__ __forceinline__ uint4 next_word(int st, int n, int k) const {
+        return k + (int)blockDim.x < n ? word(st + k + (int)blockDim.x) : make_uint4(0u, 0u, 0u, 0u);
+    }
+
+    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], uint4 w) const {
         const uint32_t v[8] = {w.x & 0xFFFFu, w.x >> 16, w.y & 0xFFFFu, w.y >> 16,
                                w.z & 0xFFFFu, w.z >> 16, w.w & 0xFFFFu, w.w >> 16};
         V3<R> s[W];
@@ -448,9 +484,14 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         if (local) {
 #pragma unroll
             for (int t = 0; t < W; t++) s[t] = sp.get((int)v[t]);
-        } else {
+        } else { // per slot: plain loads unless some lane's partner is in another rank
+            const unsigned act = __activemask();
 #pragma unroll
-            for (int t = 0; t < W; t++) s[t] = partner_cluster(v[t]);
+            for (int t = 0; t < W; t++) {
+                const bool far = (v[t] >> 14) != 0u;
+                if (__any_sync(act, far)) s[t] = far ? partner_cluster(v[t]) : sp.get((int)v[t]);
+                else s[t] = sp.get((int)v[t]);
+            }
         }
         V3<R> hb = {R(0), R(0), R(0)};
 #pragma unroll
@@ -462,11 +503,14 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         for (int col = 0; col < S.n_colours; col++) {
             R J[W], a[9];
             V3<R> h;
-            load_coef(col, S.cf.A, J, a, h);
+            load_coef(col, OFF_A, J, a, h);
             const int st = this->col_begin(col), n = this->col_size(col);
+            uint4 wn = first_word(st, n);
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
-                const V3<R> hb = gather(col, J, d);
+                const uint4 w = wn;
+                wn = next_word(st, n, k);
+                const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
                 const V3<R> as = onsite(a, s);
                 const V3<R> H = {as.x + hb.x - h.x, as.y + hb.y - h.y, as.z + hb.z - h.z};
@@ -483,12 +527,15 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         for (int col = 0; col < S.n_colours; col++) {
             R J[W], q[9];
             V3<R> h;
-            load_coef(col, S.cf.Q, J, q, h);
+            load_coef(col, OFF_Q, J, q, h);
             const int st = this->col_begin(col), n = this->col_size(col);
+            uint4 wn = first_word(st, n);
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
+                const uint4 w = wn;
+                wn = next_word(st, n, k);
                 const uint32_t dg = (uint32_t)this->device_index(col, d);
-                const V3<R> hb = gather(col, J, d);
+                const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
                 const V3<R> hext = {hb.x - h.x, hb.y - h.y, hb.z - h.z};
                 const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
@@ -515,11 +562,14 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         for (int col = 0; col < S.n_colours; col++) {
             R J[W], m[9];
             V3<R> h;
-            load_coef(col, S.cf.E2, J, m, h);
+            load_coef(col, OFF_E2, J, m, h);
             const int st = this->col_begin(col), n = this->col_size(col);
+            uint4 wn = first_word(st, n);
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
-                const V3<R> hb = gather(col, J, d);
+                const uint4 w = wn;
+                wn = next_word(st, n, k);
+                const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
                 e += (double)(dot(s, onsite(m, s)) - dot(s, h)) + 0.5 * (double)dot(s, hb);
             }
@@ -658,7 +708,7 @@ __global__ void __launch_bounds__(NT, 1)
         const double T = rd.T_override > 0 ? rd.T_override : cs.T_slot[slot];
         if (threadIdx.x == 0) s_sigma = rd.reset_sigma ? rd.sigma0 : cs.sigma_slot[slot];
         __syncthreads();
-        const K k(S, sp, sync, c, slot, rank, s_coef, words ? swords : gwords);
+        const K k(S, sp, sync, c, slot, rank, s_coef, words ? swords : gwords, words);
         k.prepare();
         const R invT = (R)(1.0 / T);
         const bool writer = threadIdx.x == 0 && rank == 0;

@@ -389,6 +389,30 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     return {"energy": E, "magnetization": M, "summary": summarize(mc, E, M)}
 
 
+def autotune(mc: MonteCarlo, n_windows: int = 4, alg: _Alg | None = None) -> list[dict]:
+    """Time the resident kernel's launch configurations (CTAs per replica,
+    threads per CTA) on this MonteCarlo's replicas with its PT schedule, keep
+    the fastest for later runs, and return the candidates.  The replicas and
+    every counter are restored exactly, so the chain is unaffected.  No
+    counterpart in the reference (its knobs are this library's)."""
+    alg = Metropolis() if alg is None else alg
+    p = mc.parameters
+    rp = _lib.RunParams()
+    rp.sweep_start = 0
+    rp.n_sweeps = 0
+    rp.t_thermalization = p.t_thermalization
+    rp.overrelaxation_rate = p.overrelaxation_rate
+    rp.swap_rate = p.swap_rate if mc.n_replicas > 1 else 0
+    rp.probe_rate = p.probe_rate
+    rp.kind = alg.kind
+    rp.path = _PATHS[mc.path]
+    entries = (_lib.TuneEntry * 8)()
+    n = C.c_int32()
+    mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, 8, C.byref(n))
+    return [{"cluster": e.cluster, "block": e.block, "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)}
+            for e in entries[:n.value]]
+
+
 def _print_runtime_statistics(mc, t, acc, exc, n):
     """print_runtime_statistics! (helper.jl:25-78), one line per replica."""
     p = mc.parameters

@@ -125,7 +125,8 @@ typedef struct {
     int32_t probe_rate;       /* <= 0: no probes */
     int32_t kind;             /* CSMC_METROPOLIS* */
     int32_t path;             /* CSMC_PATH_* */
-    int32_t resident_block;   /* threads per CTA of the resident kernel: 512 or 1024; 0 = automatic */
+    int32_t resident_block;   /* threads per CTA of the resident kernel: a multiple of 32, capped at the
+                                 kernel's largest (896 or 512); 0 = automatic (balanced, or the autotuner's) */
     double *probe_energy;     /* [probe_capacity][n_slots] or NULL */
     double *probe_magnetization; /* [probe_capacity][n_slots] or NULL */
     int64_t probe_capacity;
@@ -263,6 +264,24 @@ int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_therm
  * this library; no counterpart in the reference. */
 int csmc_set_cluster_size(void *ctx, int32_t ranks);
 int csmc_cluster_size(void *ctx, int32_t *ranks);
+
+/* Autotuner of the resident kernel's launch configuration (no counterpart in
+ * the reference; the tuning knobs are this library's).  For every cluster size
+ * that fits (1, 2 or 4 CTAs per replica) and two block sizes (the balanced one
+ * and the kernel's largest), it times n_windows exchange windows of the
+ * schedule in *params on the context's own replicas, restores the replicas and
+ * every counter exactly (the chain continues as if no tuning had happened),
+ * and keeps the fastest configuration for later runs.  entries[capacity]
+ * receives the candidates with their device time per window; n_entries the
+ * number of candidates (0 when the lattices run on the global path). */
+typedef struct {
+    int32_t cluster;       /* CTAs per replica */
+    int32_t block;         /* threads per CTA */
+    double ms_per_window;  /* device time of one exchange window */
+    int32_t chosen;        /* 1 for the configuration kept */
+} csmc_tune_entry;
+int csmc_autotune(void *ctx, const csmc_run_params *params, int32_t n_windows, csmc_tune_entry *entries,
+                  int32_t capacity, int32_t *n_entries);
 
 /* Spin-length renormalisation interval of the single-precision kernels, in
  * sweeps (0 = never).  Default 64. */

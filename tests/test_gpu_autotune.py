@@ -1,0 +1,54 @@
+"""csmc_autotune: the launch-configuration autotuner of the resident kernel.
+
+It times every cluster size that fits and two block sizes on the context's
+own replicas, then restores the replicas and counters exactly, so a chain that
+was tuned before running equals one that was not (same tolerances as the
+cluster-size equality test: the configurations run the same arithmetic per
+site).
+"""
+import numpy as np
+import pytest
+
+from test_gpu_parity import rand_spins, setup
+
+pytestmark = pytest.mark.gpu
+
+
+def _pt(m, mc, lat, tune):
+    mc.ctx.set_temperatures(np.array([0.2, 0.4, 0.8, 1.6]))
+    for r in range(4):
+        mc.set_spins(rand_spins(lat.size, 40 + r), r)
+    mc.path = "resident"
+    p = mc.parameters
+    p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 5, 35, 40, 10
+    p.probe_rate, p.swap_rate, p.overrelaxation_rate = 5, 5, 5
+    entries = m.autotune(mc, n_windows=2, alg=m.MetropolisAdaptive()) if tune else []
+    out = m.parallel_tempering(mc, alg=m.MetropolisAdaptive(), verbose=False)
+    return entries, (np.stack([mc.spins(r) for r in range(4)]), out["energy"], out["magnetization"],
+                     mc.accepted.copy(), mc.exchanged.copy(), np.atleast_1d(mc.sigma))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["sc", "honeycomb"])
+def test_autotune_leaves_the_chain_unchanged(m, orc, name, precision):
+    lat, _, mc0 = setup(m, orc, name, precision, R=4, seed=9)
+    _, ref = _pt(m, mc0, lat, tune=False)
+    lat, _, mc1 = setup(m, orc, name, precision, R=4, seed=9)
+    entries, got = _pt(m, mc1, lat, tune=True)
+    assert len(entries) >= 1 and sum(e["chosen"] for e in entries) == 1
+    assert all(e["ms_per_window"] > 0 and e["block"] % 32 == 0 for e in entries)
+    assert {e["cluster"] for e in entries} <= {1, 2, 4}
+    assert np.abs(ref[0] - got[0]).max() <= 1e-12 * (1 if precision == "fp64" else 1e6)
+    assert np.abs(ref[1] - got[1]).max() <= 1e-9 * lat.size
+    assert np.abs(ref[2] - got[2]).max() <= 1e-9 * lat.size
+    assert np.array_equal(ref[3], got[3]) and np.array_equal(ref[4], got[4])
+    assert np.allclose(ref[5], got[5], rtol=1e-12)
+
+
+def test_autotune_on_the_global_path_is_a_no_op(m, orc):
+    """A run that takes the global path has no resident configuration to tune."""
+    lat, _, mc = setup(m, orc, "pyrochlore", "fp32", R=2, seed=3)
+    mc.path = "global"
+    before = mc.spins(1).copy()
+    assert m.autotune(mc, n_windows=1) == []
+    assert np.array_equal(mc.spins(1), before)
