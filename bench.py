@@ -9,10 +9,11 @@ every 10 sweeps, probes every 10 sweeps.  Spins, fields and dE in FP32;
 energies, the exchange exponent and observables in FP64.  Synthetic: random
 initial spins from the Philox INIT stream.
 
-One step = one exchange window of the reference's loop (monte_carlo.jl:295-388):
-10 iterations = 10 overrelaxation + 2 Metropolis sweeps of all 64 replicas,
-the energies, one replica exchange and one probe (E, |M|).
-Site updates per step = 64 * 13824 * 12.
+One step = 100 iterations of the reference's loop (monte_carlo.jl:295-388):
+10 exchange windows, each 10 overrelaxation + 2 Metropolis sweeps of all 64
+replicas, the energies, one replica exchange and one probe (E, |M|) -- one
+csmc_run call, as a caller running report_interval >= 100 makes.
+Site updates per step = 64 * 13824 * 120.
 
 `value` is device throughput (CUDA events on the library's stream) with the
 replicas resident in HBM; L2 is flushed (256 MB write) between steps.
@@ -48,7 +49,7 @@ sys.path.insert(0, str(ROOT))
 import __graft_entry__ as G  # noqa: E402
 
 L_SIDE, R_REPL, OR_RATE, SWAP_RATE, PROBE_RATE = 24, 64, 5, 10, 10
-ITER_PER_STEP = 10
+ITER_PER_STEP = 100
 SEED = 20261203
 BYTES_PER_UPDATE_FP32 = 12 * (2 + 6)  # s_b * (2 + z): own spin read+write, 6 neighbours read
 RESIDENT_BLOCK = 0
@@ -153,16 +154,18 @@ def bench_ours(args, rank, world, dist):
     ctx.set_temperatures(temperatures())
     ctx.call("csmc_random_spins", C.c_uint64(SEED + 1000 * rank))
     tuned = []
+    if args.no_persistent:
+        ctx.call("csmc_set_persistent", 0)
     if args.cluster:
         ctx.call("csmc_set_cluster_size", args.cluster)
     elif not args.no_autotune and not args.block:
         # the library's autotuner picks CTAs per replica and threads per CTA on
         # these replicas (state restored exactly afterwards)
-        entries = (L.TuneEntry * 8)()
+        entries = (L.TuneEntry * 16)()
         n = C.c_int32()
-        ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 8, C.byref(n))
-        tuned = [{"cluster": e.cluster, "block": e.block, "ms_per_window": round(e.ms_per_window, 5),
-                  "chosen": bool(e.chosen)} for e in entries[:n.value]]
+        ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 16, C.byref(n))
+        tuned = [{"cluster": e.cluster, "block": e.block, "persistent": bool(e.persistent),
+                  "ms_per_window": round(e.ms_per_window, 5), "chosen": bool(e.chosen)} for e in entries[:n.value]]
     ranks = C.c_int32()
     ctx.call("csmc_cluster_size", C.byref(ranks))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -250,7 +253,8 @@ def bench_ours(args, rank, world, dist):
         ctx64.call("csmc_run", C.byref(run_params(L, 1, ITER_PER_STEP, path=L.PATH_PER_REPLICA)))
         t = 0.0
         for k in range(args.plain_steps):
-            ctx64.call("csmc_run", C.byref(run_params(L, 11 + 10 * k, ITER_PER_STEP, path=L.PATH_PER_REPLICA)))
+            ctx64.call("csmc_run", C.byref(run_params(L, 1 + ITER_PER_STEP * (k + 1), ITER_PER_STEP,
+                                                      path=L.PATH_PER_REPLICA)))
             t += stats(ctx64)[0] / 1e3
         out["plain_fp64_per_replica"] = {"value": upd * args.plain_steps / t, "unit": "site updates/s",
                                          "ms_per_step": 1e3 * t / args.plain_steps,
@@ -392,6 +396,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: autotuned; 1, 2 or 4)")
     ap.add_argument("--no-autotune", action="store_true", help="skip csmc_autotune (library heuristics)")
+    ap.add_argument("--no-persistent", action="store_true",
+                    help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",
                     choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
                              "pyrochlore_large_fp32"],

@@ -64,7 +64,8 @@ class RunParams(C.Structure):
 
 
 class TuneEntry(C.Structure):
-    _fields_ = [("cluster", C.c_int32), ("block", C.c_int32), ("ms_per_window", C.c_double), ("chosen", C.c_int32)]
+    _fields_ = [("cluster", C.c_int32), ("block", C.c_int32), ("persistent", C.c_int32),
+                ("ms_per_window", C.c_double), ("chosen", C.c_int32)]
 
 
 # name -> (restype, argtypes); every entry point declared in include/csmc.h
@@ -106,6 +107,8 @@ SIGNATURES = {
     "csmc_set_cluster_size": (C.c_int, [_vp, C.c_int32]),
     "csmc_cluster_size": (C.c_int, [_vp, i32p]),
     "csmc_autotune": (C.c_int, [_vp, C.POINTER(RunParams), C.c_int32, C.POINTER(TuneEntry), C.c_int32, i32p]),
+    "csmc_set_persistent": (C.c_int, [_vp, C.c_int32]),
+    "csmc_persistent": (C.c_int, [_vp, i32p]),
     "csmc_set_renormalize": (C.c_int, [_vp, C.c_int32]),
     "csmc_spin_length_drift": (C.c_int, [_vp, f64p]),
     "csmc_last_run_stats": (C.c_int, [_vp, f64p, i64p, f64p, i64p]),

@@ -78,6 +78,9 @@ struct System {
     ClusterLayout cl_layout;
     // bilinear partners packed 8 x 16 bit per site (specialised kernel)
     DevBuf<uint4> p2v, q2v;
+    // per-rank partner tables and local patterns (generic kernel on a cluster)
+    DevBuf<uint16_t> q2c, q3c, q4c;
+    DevBuf<uint8_t> patc;
     size_t resident_smem = 0;
     // reference-layout tables for the replay kernel (built on first use)
     DevBuf<int64_t> xbs, xcs, xqs;
@@ -98,6 +101,9 @@ struct Ctx {
     DevBuf<unsigned long long> sweep_acc;
     DevBuf<unsigned int> drift_bits;
     DevBuf<int> error_flag, work_ctr;
+    DevBuf<unsigned int> grid_bar; // arrival counter of the persistent kernel's grid barrier
+    bool persistent_ok = true;     // cleared if a cooperative launch is refused
+    bool persistent_on = true;     // csmc_set_persistent
     DevBuf<double> part, stage, rec_E, rec_M;
     DevBuf<ResSys<float>> fres;
     DevBuf<ResSys<double>> dres;
@@ -360,6 +366,10 @@ template <typename R> static ResSys<R> make_res(const System &S, const SysArgs<R
     r.p2v = S.p2v.p;
     r.q2v = S.q2v.p;
     r.pv_stage = S.pv_stage ? 1 : 0;
+    r.q2c = S.q2c.p;
+    r.q3c = S.q3c.p;
+    r.q4c = S.q4c.p;
+    r.patc = S.patc.p;
     if (L.ranks > 1)
         for (int k = 0; k < L.ranks; k++)
             for (int c = 0; c < S.plan.n_colours; c++) {
@@ -383,8 +393,6 @@ static int64_t dynamic_smem_limit(const Ctx &C) { return (int64_t)C.max_smem - 8
 // specialised kernel applies and the parts fit shared memory).
 static void choose_cluster(Ctx &C, int requested) {
     const int64_t limit = dynamic_smem_limit(C);
-    bool fast = true;
-    for (auto &S : C.sys) fast = fast && S->fast_ok;
     auto fits = [&](int c, bool prefer) {
         if (c == 1) {
             for (auto &S : C.sys)
@@ -401,11 +409,10 @@ static void choose_cluster(Ctx &C, int requested) {
     int best = 1;
     if (requested > 0) {
         require(requested == 1 || requested == 2 || requested == 4, CSMC_ERR_INVALID, "cluster size must be 1, 2 or 4");
-        require(requested == 1 || (fast && fits(requested, false)), CSMC_ERR_UNSUPPORTED,
-                "this cluster size needs lattices without cubic/quartic terms, one basis per colour class, and "
-                "parts that fit shared memory");
+        require(requested == 1 || fits(requested, false), CSMC_ERR_UNSUPPORTED,
+                "this cluster size needs parts of at most 16383 sites that fit shared memory");
         best = requested;
-    } else if (fast) {
+    } else {
         int pick = 0;
         for (int c : {1, 2, 4})
             if (fits(c, true)) pick = c;
@@ -422,7 +429,11 @@ static void choose_cluster(Ctx &C, int requested) {
         System &S = *Sp;
         if (best > 1) {
             S.cl_layout = make_cluster_layout(S.plan, best);
-            {
+            S.q2c.upload(S.cl_layout.q2);
+            S.q3c.upload(S.cl_layout.q3);
+            S.q4c.upload(S.cl_layout.q4);
+            S.patc.upload(S.cl_layout.pat);
+            if (S.fast_ok) {
                 const ClusterLayout &L = S.cl_layout;
                 const int W = std::max(S.plan.W2, 1);
                 std::vector<uint4> all;
@@ -532,6 +543,8 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     int zi = 0;
     C->error_flag.upload(&zi, 1);
     C->work_ctr.upload(&zi, 1);
+    unsigned int zu = 0;
+    C->grid_bar.upload(&zu, 1);
     size_t part = 0, stage = 0;
     for (auto &S : C->sys) {
         part = std::max(part, (size_t)(3 * S->R * partial_blocks(S->plan.Np)));
@@ -821,26 +834,54 @@ static ResidentSel resident_selection(const Ctx &C) {
     return sel;
 }
 
-static void resident_launch(Ctx &C, const RunDesc &rd, int block, Launches &L) {
+// Resident CTAs (one replica each) or clusters that fit on the device at once.
+static int resident_slots(Ctx &C, int block, size_t *smem_out) {
     size_t smem = 0;
     for (auto &S : C.sys) smem = std::max(smem, S->resident_smem);
     const ResidentSel sel = resident_selection(C);
     const int cap = C.precision == CSMC_FP32 ? resident_capacity<float>(block, smem, sel, C.n_sms)
                                              : resident_capacity<double>(block, smem, sel, C.n_sms);
     require(cap >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on the device with this shared memory size");
+    if (smem_out) *smem_out = smem;
+    return cap;
+}
+
+// One resident launch.  rd.persistent: a cooperative launch with one CTA (or
+// cluster) per replica; returns false, with nothing launched, if the device
+// refuses it.
+static bool resident_launch(Ctx &C, RunDesc rd, int block, Launches &L) {
+    size_t smem = 0;
+    const int cap = resident_slots(C, block, &smem);
+    const ResidentSel sel = resident_selection(C);
     // CTAs (one per replica) or clusters (sel.cl CTAs per replica)
     const int grid = std::min(C.n_items, cap) * std::max(sel.cl, 1);
+    if (rd.persistent) {
+        require(cap >= C.n_items, CSMC_ERR_INVALID, "persistent launch needs every replica resident at once");
+        rd.grid_bar = C.grid_bar.p;
+        rd.n_blocks = (uint32_t)grid;
+        rd.lattices = C.lattices.p;
+        rd.n_lattices = (int)C.sys.size();
+        rd.k0 = C.k0;
+        rd.k1 = C.k1;
+        CK(cudaMemsetAsync(C.grid_bar.p, 0, sizeof(unsigned int), C.st));
+    }
     auto ev = C.next_kernel_events();
     CK(cudaMemsetAsync(C.work_ctr.p, 0, sizeof(int), C.st));
     CK(cudaEventRecord(ev.first, C.st));
     cudaError_t e = C.precision == CSMC_FP32
                         ? launch_resident<float>(C.fres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid, block,
-                                                 smem, sel, C.st)
+                                                 smem, sel, rd.persistent != 0, C.st)
                         : launch_resident<double>(C.dres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid,
-                                                  block, smem, sel, C.st);
+                                                  block, smem, sel, rd.persistent != 0, C.st);
+    if (e != cudaSuccess && rd.persistent) {
+        cudaGetLastError(); // a refused cooperative launch leaves no sticky error
+        C.kev_used--;
+        return false;
+    }
     CK(e);
     CK(cudaEventRecord(ev.second, C.st));
     L.n += 1;
+    return true;
 }
 
 static void run(Ctx &C, csmc_run_params *p) {
@@ -901,10 +942,52 @@ static void run(Ctx &C, csmc_run_params *p) {
     if (path == CSMC_PATH_RESIDENT) {
         const int block = resident_block(C, p->resident_block);
         // windows end at exchange iterations; without exchanges, at most
-        // `chunk` iterations per launch
-        const int64_t chunk = 256;
+        // `chunk` iterations per launch.  With exchanges and every replica
+        // resident at once, one persistent launch runs up to kWindows windows
+        // and the exchanges between them.
+        const int64_t chunk = 256, kWindows = 128;
+        const int64_t period = s.swap_enabled ? std::lcm((int64_t)s.swap_rate, s.dosweep) : 0;
+        bool persistent = s.swap_enabled && C.persistent_on && C.persistent_ok &&
+                          resident_slots(C, block, nullptr) >= C.n_items;
         int64_t it = s.start;
         while (it < s.end) {
+            if (persistent) {
+                const int64_t q1 = (it + period - 1) / period * period;
+                const int64_t to = std::min(s.end - 1, q1 + (kWindows - 1) * period);
+                RunDesc rd{};
+                rd.it0 = it;
+                rd.it1 = to + 1;
+                rd.t_therm = s.t_therm;
+                rd.probe_first = s.probe_first;
+                rd.probe_cap = s.cap;
+                rd.rec_E = recE;
+                rd.rec_M = recM;
+                rd.msweep0 = C.msweep;
+                rd.or_rate = s.or_rate;
+                rd.swap_rate = s.swap_rate;
+                rd.probe_rate = s.probe_rate;
+                rd.kind = s.kind;
+                rd.n_slots = n_slots;
+                rd.renorm_every = C.renorm_every;
+                rd.sweeps0 = C.nsweeps;
+                rd.swap_enabled = 1;
+                rd.persistent = 1;
+                rd.swap_period = period;
+                if (!resident_launch(C, rd, block, L)) {
+                    persistent = false; // the device refused the cooperative launch: one launch per window
+                    C.persistent_ok = false;
+                    continue;
+                }
+                for (int64_t q = it; q <= to; q++) {
+                    if (s.is_metro(q)) {
+                        C.msweep++;
+                        C.nsweeps++;
+                    }
+                    if (s.or_rate != 0) C.nsweeps++;
+                }
+                it = to + 1;
+                continue;
+            }
             int64_t to = std::min(s.end, it + chunk) - 1;
             bool ends_swap = false;
             if (s.swap_enabled) {
@@ -1550,10 +1633,11 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
     q.accepted = q.exchanged = nullptr;
     const int span = q.swap_rate > 0 ? q.swap_rate : std::max(q.overrelaxation_rate, 1) * 10;
     q.n_sweeps = (int64_t)n_windows * span;
-    const int cl0 = C.cl, bp0 = C.block_pref;
+    const bool allow_persistent = C.persistent_on && C.persistent_ok; // csmc_set_persistent(0) is respected
     StateCopy saved(C);
     struct Cand {
         int cl, block;
+        bool persistent;
         double ms;
     };
     std::vector<Cand> cands;
@@ -1570,28 +1654,33 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
         C.block_pref = 0;
         const ResidentSel sel = resident_selection(C);
         const int balanced = resident_block(C, 0), largest = resident_max_threads(sel.fast, sel.bil, sel.ons);
-        for (int block : {balanced, largest}) {
-            if (block == largest && largest == balanced && !cands.empty() && cands.back().cl == cl) continue;
-            C.block_pref = block;
-            run(C, &q); // warm-up (first launch of this kernel)
-            saved.restore(C);
-            run(C, &q);
-            cands.push_back({cl, block, C.last_ms / n_windows});
-            saved.restore(C);
+        std::vector<int> blocks{balanced};
+        if (largest != balanced) blocks.push_back(largest);
+        for (int block : blocks) {
+            for (bool pers : {true, false}) {
+                if (pers && !(allow_persistent && C.persistent_ok)) continue;
+                C.block_pref = block;
+                C.persistent_on = pers;
+                run(C, &q); // warm-up (first launch of this configuration)
+                saved.restore(C);
+                run(C, &q);
+                cands.push_back({cl, block, pers && C.persistent_ok, C.last_ms / n_windows});
+                saved.restore(C);
+            }
         }
     }
     require(!cands.empty(), CSMC_ERR_UNSUPPORTED, "no resident configuration fits these lattices");
     size_t best = 0;
     for (size_t k = 1; k < cands.size(); k++)
         if (cands[k].ms < cands[best].ms) best = k;
-    (void)cl0;
-    (void)bp0;
     choose_cluster(C, cands[best].cl);
     upload_resident(C);
     C.block_pref = cands[best].block;
+    C.persistent_on = cands[best].persistent;
     for (size_t k = 0; k < cands.size() && (int)k < capacity; k++) {
         out[k].cluster = cands[k].cl;
         out[k].block = cands[k].block;
+        out[k].persistent = cands[k].persistent ? 1 : 0;
         out[k].ms_per_window = cands[k].ms;
         out[k].chosen = k == best ? 1 : 0;
     }
@@ -1609,6 +1698,20 @@ int csmc_autotune(void *c, const csmc_run_params *params, int32_t n_windows, csm
     CK(cudaStreamSynchronize(C.st));
     autotune(C, params, n_windows, entries, capacity, &n);
     *n_entries = n;
+    API_END
+}
+
+int csmc_set_persistent(void *c, int32_t on) {
+    API_BEGIN
+    ctx_of(c).persistent_on = on != 0;
+    API_END
+}
+
+int csmc_persistent(void *c, int32_t *on) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(on != nullptr, CSMC_ERR_INVALID, "on is NULL");
+    *on = C.persistent_on && C.persistent_ok ? 1 : 0;
     API_END
 }
 

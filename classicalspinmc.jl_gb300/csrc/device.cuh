@@ -71,6 +71,43 @@ template <typename R> struct V3 {
     R x, y, z;
 };
 
+// Arithmetic with explicit rounding: every product, sum and fused
+// multiply-add below is spelled out, so the compiler cannot contract or
+// re-associate differently in different kernels.  The resident kernel's
+// instantiations (one CTA or a cluster per replica) and the colour-sweep
+// kernels therefore compute bit-identical values for the same site.
+template <typename R> struct Fp;
+template <> struct Fp<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+template <> struct Fp<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+};
+// acc + M s, one fused multiply-add per term in the order M[0] s.x, M[1] s.y,
+// M[2] s.z (a matrix c*I gives exactly acc + c s)
+template <typename R> __device__ __forceinline__ V3<R> add_matvec(V3<R> acc, const R *M, V3<R> s) {
+    using F = Fp<R>;
+    return {F::fma(M[2], s.z, F::fma(M[1], s.y, F::fma(M[0], s.x, acc.x))),
+            F::fma(M[5], s.z, F::fma(M[4], s.y, F::fma(M[3], s.x, acc.y))),
+            F::fma(M[8], s.z, F::fma(M[7], s.y, F::fma(M[6], s.x, acc.z)))};
+}
+template <typename R> __device__ __forceinline__ V3<R> add_scaled(V3<R> acc, R c, V3<R> s) {
+    using F = Fp<R>;
+    return {F::fma(c, s.x, acc.x), F::fma(c, s.y, acc.y), F::fma(c, s.z, acc.z)};
+}
+template <typename R> __device__ __forceinline__ V3<R> vadd(V3<R> a, V3<R> b) {
+    return {Fp<R>::add(a.x, b.x), Fp<R>::add(a.y, b.y), Fp<R>::add(a.z, b.z)};
+}
+template <typename R> __device__ __forceinline__ V3<R> vsub(V3<R> a, V3<R> b) {
+    return {Fp<R>::sub(a.x, b.x), Fp<R>::sub(a.y, b.y), Fp<R>::sub(a.z, b.z)};
+}
+
 // The spins of one replica in device memory.  Single precision: one float4
 // (x, y, z, 0) per device site, so a site is a single 16-byte load and a
 // replica one contiguous block of 16 * Np bytes.  Double precision: three
@@ -124,29 +161,25 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     for (int t = 0; t < tb.W2; t++) {
         const int64_t j = tb.p2[t * Np + d];
         const R *M = cf.mats + 9 * cf.c2[b * tb.W2 + t];
-        const V3<R> sj = sv.get(j);
-        const R sx = sj.x, sy = sj.y, sz = sj.z;
-        hb.x += M[0] * sx + M[1] * sy + M[2] * sz;
-        hb.y += M[3] * sx + M[4] * sy + M[5] * sz;
-        hb.z += M[6] * sx + M[7] * sy + M[8] * sz;
+        hb = add_matvec(hb, M, sv.get(j));
     }
     if (CUB) {
         for (int t = 0; t < tb.W3; t++) {
             const int64_t j = tb.p3[(2 * t) * Np + d], k = tb.p3[(2 * t + 1) * Np + d];
             const R *C = cf.cubs + 27 * cf.c3[b * tb.W3 + t];
             const V3<R> sj = sv.get(j), sk = sv.get(k);
+            using F = Fp<R>;
             const R a0 = sj.x, a1 = sj.y, a2 = sj.z, b0 = sk.x, b1 = sk.y, b2 = sk.z;
-            R o[9] = {a0 * b0, a0 * b1, a0 * b2, a1 * b0, a1 * b1, a1 * b2, a2 * b0, a2 * b1, a2 * b2};
+            const R o[9] = {F::mul(a0, b0), F::mul(a0, b1), F::mul(a0, b2), F::mul(a1, b0), F::mul(a1, b1),
+                            F::mul(a1, b2), F::mul(a2, b0), F::mul(a2, b1), F::mul(a2, b2)};
             R sx = 0, sy = 0, sz = 0;
 #pragma unroll
             for (int q = 0; q < 9; q++) {
-                sx += C[q] * o[q];
-                sy += C[9 + q] * o[q];
-                sz += C[18 + q] * o[q];
+                sx = F::fma(C[q], o[q], sx);
+                sy = F::fma(C[9 + q], o[q], sy);
+                sz = F::fma(C[18 + q], o[q], sz);
             }
-            hc.x += sx;
-            hc.y += sy;
-            hc.z += sz;
+            hc = vadd(hc, V3<R>{sx, sy, sz});
         }
     }
     if (QUA) {
@@ -155,33 +188,37 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
             const R *Q = cf.quas + 81 * cf.c4[b * tb.W4 + t];
             const V3<R> sj = sv.get(j), sk = sv.get(k), sl = sv.get(l);
             const R a[3] = {sj.x, sj.y, sj.z}, bb[3] = {sk.x, sk.y, sk.z}, c[3] = {sl.x, sl.y, sl.z};
+            using F = Fp<R>;
             R sx = 0, sy = 0, sz = 0;
 #pragma unroll
             for (int p = 0; p < 3; p++)
 #pragma unroll
                 for (int q = 0; q < 3; q++) {
-                    const R ab = a[p] * bb[q];
+                    const R ab = F::mul(a[p], bb[q]);
 #pragma unroll
                     for (int r = 0; r < 3; r++) {
-                        const R o = ab * c[r];
+                        const R o = F::mul(ab, c[r]);
                         const int idx = (p * 3 + q) * 3 + r;
-                        sx += Q[idx] * o;
-                        sy += Q[27 + idx] * o;
-                        sz += Q[54 + idx] * o;
+                        sx = F::fma(Q[idx], o, sx);
+                        sy = F::fma(Q[27 + idx], o, sy);
+                        sz = F::fma(Q[54 + idx], o, sz);
                     }
                 }
-            hq.x += sx;
-            hq.y += sy;
-            hq.z += sz;
+            hq = vadd(hq, V3<R>{sx, sy, sz});
         }
     }
 }
 
 template <typename R> __device__ __forceinline__ V3<R> matvec(const R *M, V3<R> s) {
-    return {M[0] * s.x + M[1] * s.y + M[2] * s.z, M[3] * s.x + M[4] * s.y + M[5] * s.z,
-            M[6] * s.x + M[7] * s.y + M[8] * s.z};
+    using F = Fp<R>;
+    return {F::fma(M[2], s.z, F::fma(M[1], s.y, F::mul(M[0], s.x))),
+            F::fma(M[5], s.z, F::fma(M[4], s.y, F::mul(M[3], s.x))),
+            F::fma(M[8], s.z, F::fma(M[7], s.y, F::mul(M[6], s.x)))};
 }
-template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) {
+    using F = Fp<R>;
+    return F::fma(a.z, b.z, F::fma(a.y, b.y, F::mul(a.x, b.x)));
+}
 
 // get_local_field (hamiltonian.jl:3-67): 2 O s + (self loops) + partners - h.
 template <typename R, typename Idx, bool CUB, bool QUA, class SV>
@@ -190,9 +227,9 @@ __device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &
     partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
     const V3<R> s = sv.get(d);
     const V3<R> os = matvec(cf.O + 9 * b, s), ps = matvec(cf.P + 9 * b, s);
-    const R *h = cf.h + 3 * b;
-    return {R(2) * os.x + ps.x + hb.x + hc.x + hq.x - h[0], R(2) * os.y + ps.y + hb.y + hc.y + hq.y - h[1],
-            R(2) * os.z + ps.z + hb.z + hc.z + hq.z - h[2]};
+    const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
+    const V3<R> two_os = {Fp<R>::mul(R(2), os.x), Fp<R>::mul(R(2), os.y), Fp<R>::mul(R(2), os.z)};
+    return vsub(vadd(vadd(vadd(vadd(two_os, ps), hb), hc), hq), h);
 }
 
 // Energy of moving site d from s to sn with all other spins fixed:
@@ -200,13 +237,13 @@ __device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &
 // dE = sn.Q.sn - s.Q.s + (sn - s).hext.
 template <typename R>
 __device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn, V3<R> hext) {
+    using F = Fp<R>;
     const R *O = cf.O + 9 * b, *P = cf.P + 9 * b;
     R q[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) q[k] = O[k] + P[k];
+    for (int k = 0; k < 9; k++) q[k] = F::add(O[k], P[k]);
     const R en = dot(sn, matvec(q, sn)), eo = dot(s, matvec(q, s));
-    const V3<R> ds = {sn.x - s.x, sn.y - s.y, sn.z - s.z};
-    return (en - eo) + dot(ds, hext);
+    return F::add(F::sub(en, eo), dot(vsub(sn, s), hext));
 }
 
 // Contribution of site d to total_energy (hamiltonian.jl:70-132):
@@ -214,16 +251,17 @@ __device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn
 template <typename R, typename Idx, bool CUB, bool QUA, class SV>
 __device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d,
                                                     int b) {
+    using F = Fp<double>;
     V3<R> hb, hc, hq;
     partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
     const V3<R> s = sv.get(d);
-    const R *h = cf.h + 3 * b;
-    const R eo = dot(s, matvec(cf.O + 9 * b, s));
-    const R ep = dot(s, matvec(cf.P + 9 * b, s));
-    const R ez = s.x * h[0] + s.y * h[1] + s.z * h[2];
-    double e = -(double)ez + (double)eo + 0.5 * ((double)dot(s, hb) + (double)ep);
-    if (CUB) e += (double)dot(s, hc) / 3.0;
-    if (QUA) e += 0.25 * (double)dot(s, hq);
+    const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
+    const double eo = (double)dot(s, matvec(cf.O + 9 * b, s));
+    const double ep = (double)dot(s, matvec(cf.P + 9 * b, s));
+    const double ez = (double)dot(s, h);
+    double e = F::add(F::sub(eo, ez), F::mul(0.5, F::add((double)dot(s, hb), ep)));
+    if (CUB) e = F::add(e, (double)dot(s, hc) / 3.0);
+    if (QUA) e = F::fma(0.25, (double)dot(s, hq), e);
     return e;
 }
 
@@ -251,6 +289,21 @@ template <> struct Math<double> {
     static __device__ __forceinline__ double exp_(double v) { return exp(v); }
     static __device__ __forceinline__ double div_(double a, double b) { return a / b; }
 };
+
+// Overrelaxation (monte_carlo.jl:135-137): s <- -s + 2 (s.H)/|H|^2 H, with
+// explicit rounding; `fast` uses the single-precision fast division.
+template <typename R> __device__ __forceinline__ V3<R> reflect(V3<R> s, V3<R> H, bool fast) {
+    using F = Fp<R>;
+    const R num = F::mul(R(2), dot(s, H)), den = dot(H, H);
+    const R proj = fast ? Math<R>::div_(num, den) : num / den;
+    return {F::fma(proj, H.x, -s.x), F::fma(proj, H.y, -s.y), F::fma(proj, H.z, -s.z)};
+}
+// The exponent -dE/T of the acceptance test (metropolis.jl:73): by the
+// reciprocal temperature in single precision, by division in double.
+template <typename R> __device__ __forceinline__ R boltz_arg(R dE, R invT, double T) {
+    if (sizeof(R) == 4) return Fp<R>::mul(-dE, invT);
+    return -dE / (R)T;
+}
 
 // Uniforms of one Metropolis proposal from the Philox stream keyed by the
 // context seed; counter = (device site, Metropolis sweep, replica, purpose).
@@ -282,16 +335,17 @@ template <> struct Draw<double> {
 // (metropolis.jl:84-87) for uniforms (uphi, uz).
 template <typename R>
 __device__ __forceinline__ V3<R> propose(int kind, R S, R sigma, V3<R> s, R uphi, R uz) {
+    using F = Fp<R>;
     R sp, cp;
     Math<R>::sincospi2(uphi, &sp, &cp);
-    const R zz = R(2) * uz - R(1);
-    R r2 = R(1) - zz * zz;
+    const R zz = F::sub(F::mul(R(2), uz), R(1));
+    const R r2 = F::sub(R(1), F::mul(zz, zz));
     const R r = Math<R>::sqrt_(r2 > R(0) ? r2 : R(0));
-    V3<R> u = {S * (r * cp), S * (r * sp), S * zz};
+    const V3<R> u = {F::mul(S, F::mul(r, cp)), F::mul(S, F::mul(r, sp)), F::mul(S, zz)};
     if (kind == CSMC_METROPOLIS) return u;
-    V3<R> v = {s.x + sigma * u.x, s.y + sigma * u.y, s.z + sigma * u.z};
-    const R inv = S * Math<R>::rsqrt_(v.x * v.x + v.y * v.y + v.z * v.z);
-    return {v.x * inv, v.y * inv, v.z * inv};
+    const V3<R> v = vadd(s, V3<R>{F::mul(sigma, u.x), F::mul(sigma, u.y), F::mul(sigma, u.z)});
+    const R inv = F::mul(S, Math<R>::rsqrt_(dot(v, v)));
+    return {F::mul(v.x, inv), F::mul(v.y, inv), F::mul(v.z, inv)};
 }
 
 } // namespace csmc

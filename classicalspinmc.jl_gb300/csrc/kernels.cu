@@ -40,14 +40,13 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
         const int b = a.tb.pat[d];
         V3<R> hb, hc, hq;
         partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
-        const R *h = a.cf.h + 3 * b;
-        const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+        const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
         const V3<R> s = p.get(d);
         const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1);
         const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
         bool accept = dE < R(0);
-        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(-dE / (R)T);
+        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(boltz_arg(dE, (R)(1.0 / T), T));
         if (accept) {
             p.set(d, sn);
             acc = 1;
@@ -68,9 +67,7 @@ __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, i
     const int b = a.tb.pat[d];
     const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
-    const V3<R> s = p.get(d);
-    const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
-    p.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
+    p.set(d, reflect(p.get(d), H, false));
 }
 
 // deterministic_updates! body (monte_carlo.jl:205-210) on one colour class.
@@ -176,36 +173,10 @@ __global__ void k_exchange(ChainState cs, const int2 *lattices, int64_t it, int 
                            int do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots) {
     const int sys = blockIdx.x;
     const int slot_base = lattices[sys].x, n_rep = lattices[sys].y;
-    if (do_swap && n_rep >= 2) {
-        const int phase = (int)((it / swap_rate) % 2);
-        for (int m = threadIdx.x; phase + 2 * m + 1 < n_rep; m += blockDim.x) {
-            const int a = phase + 2 * m, b = a + 1;
-            const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
-            const int sa = slot_base + a, sb = slot_base + b;
-            const int se = slot_base + ev, so = slot_base + od;
-            const double Te = cs.T_slot[se], To = cs.T_slot[so];
-            const double Ee = cs.E_chain[cs.chain_of[se]], Eo = cs.E_chain[cs.chain_of[so]];
-            const double x = exp((1 / To - 1 / Te) * (Eo - Ee));
-            const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, (uint32_t)sys ^ (uint32_t)(it >> 32), PURPOSE_SWAP,
-                                       k0, k1);
-            if (u53(w.x, w.y) < (x < 1.0 ? x : 1.0)) {
-                const int ca = cs.chain_of[sa], cb = cs.chain_of[sb];
-                cs.chain_of[sa] = cb;
-                cs.chain_of[sb] = ca;
-                cs.slot_of[cb] = sa;
-                cs.slot_of[ca] = sb;
-                cs.exch_slot[sa] += 1;
-                cs.exch_slot[sb] += 1;
-            }
-        }
-    }
+    if (do_swap) exchange_slots(cs, sys, slot_base, n_rep, it, swap_rate, k0, k1);
     if (kq < 0) return;
     __syncthreads();
-    for (int q = threadIdx.x; q < n_rep; q += blockDim.x) {
-        const int slot = slot_base + q, c = cs.chain_of[slot];
-        if (rec_E) rec_E[kq * n_slots + slot] = cs.E_chain[c];
-        if (rec_M) rec_M[kq * n_slots + slot] = cs.M_chain[c];
-    }
+    record_slots(cs, slot_base, n_rep, rec_E, rec_M, kq, n_slots);
 }
 
 // Reference layout (interleaved FP64, reference order) <-> device order.
@@ -272,8 +243,7 @@ __global__ void k_energy_diff(SysArgs<R> a, int r, int64_t n, const int64_t *sit
     const int b = a.tb.pat[d];
     V3<R> hb, hc, hq;
     partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
-    const R *h = a.cf.h + 3 * b;
-    const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+    const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
     const V3<R> s = p.get(d);
     const V3<R> sn = {(R)ns[3 * q], (R)ns[3 * q + 1], (R)ns[3 * q + 2]};
     dE[q] = (double)delta_e<R>(a.cf, b, s, sn, hext);

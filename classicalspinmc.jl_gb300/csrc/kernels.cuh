@@ -60,6 +60,10 @@ template <typename R> struct ResSys {
     // reading CTA's own shared memory have the top two bits clear; used by
     // the specialised kernel
     const uint4 *p2v, *q2v;
+    // generic kernel on a cluster: each rank's partner tables (cubic and
+    // quartic too, same encoding) and the pattern of its local sites
+    const uint16_t *q2c, *q3c, *q4c;
+    const uint8_t *patc;
     // nonzero: the specialised kernel stages the CTA's partner words in
     // shared memory too (they fit beside the spins)
     int32_t pv_stage;
@@ -102,6 +106,61 @@ struct RunDesc {
     int32_t renorm_every;     // single precision: renormalise every k sweeps
     uint64_t sweeps0;         // the context's sweeps (all kinds) before this launch
     int32_t swap_enabled;
+    // persistent mode: the launch covers every window of [it0, it1) (a window
+    // ends at an exchange iteration, a multiple of swap_period); between
+    // windows all CTAs meet at a grid barrier, block 0 runs the exchange of
+    // every lattice and the probe record, and all CTAs meet again
+    int32_t persistent;
+    int32_t n_lattices;
+    int64_t swap_period;      // lcm(swap_rate, max(or_rate, 1)): iterations that exchange
+    const int2 *lattices;     // per lattice {first slot, replicas}
+    uint32_t k0, k1;          // the context's Philox key (exchange streams)
+    unsigned int *grid_bar;   // grid barrier arrival counter, zero at launch
+    uint32_t n_blocks;        // CTAs in the launch
 };
+
+// Replica exchange of one lattice's slots at iteration `it`
+// (monte_carlo.jl:308-349), by all threads of one block: pairs
+// (a, a+1) with a = (it/swap_rate) % 2 + 2m are disjoint and decided in
+// parallel; the even slot of a pair accepts with probability
+// min(1, exp((1/T_odd - 1/T_even)(E_odd - E_even))) from the Philox SWAP
+// stream; an accepted exchange swaps which replica sits in the two slots.
+// Loads bypass L1: in the persistent kernel other blocks wrote these values.
+__device__ __forceinline__ void exchange_slots(const ChainState &cs, int sys, int slot_base, int n_rep, int64_t it,
+                                               int swap_rate, uint32_t k0, uint32_t k1) {
+    if (n_rep < 2) return;
+    const int phase = (int)((it / swap_rate) % 2);
+    for (int m = threadIdx.x; phase + 2 * m + 1 < n_rep; m += blockDim.x) {
+        const int a = phase + 2 * m, b = a + 1;
+        const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
+        const int sa = slot_base + a, sb = slot_base + b;
+        const int se = slot_base + ev, so = slot_base + od;
+        const double Te = __ldcg(cs.T_slot + se), To = __ldcg(cs.T_slot + so);
+        const double Ee = __ldcg(cs.E_chain + __ldcg(cs.chain_of + se));
+        const double Eo = __ldcg(cs.E_chain + __ldcg(cs.chain_of + so));
+        const double x = exp((1 / To - 1 / Te) * (Eo - Ee));
+        const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, (uint32_t)sys ^ (uint32_t)(it >> 32), PURPOSE_SWAP, k0, k1);
+        if (u53(w.x, w.y) < (x < 1.0 ? x : 1.0)) {
+            const int ca = __ldcg(cs.chain_of + sa), cb = __ldcg(cs.chain_of + sb);
+            cs.chain_of[sa] = cb;
+            cs.chain_of[sb] = ca;
+            cs.slot_of[cb] = sa;
+            cs.slot_of[ca] = sb;
+            cs.exch_slot[sa] = __ldcg(cs.exch_slot + sa) + 1;
+            cs.exch_slot[sb] = __ldcg(cs.exch_slot + sb) + 1;
+        }
+    }
+}
+
+// Probe record kq of one lattice's slots (monte_carlo.jl:368-370): the energy
+// of the last Metropolis sweep and |M| of the replica in each slot.
+__device__ __forceinline__ void record_slots(const ChainState &cs, int slot_base, int n_rep, double *rec_E,
+                                             double *rec_M, int64_t kq, int n_slots) {
+    for (int q = threadIdx.x; q < n_rep; q += blockDim.x) {
+        const int slot = slot_base + q, c = __ldcg(cs.chain_of + slot);
+        if (rec_E) rec_E[kq * n_slots + slot] = __ldcg(cs.E_chain + c);
+        if (rec_M) rec_M[kq * n_slots + slot] = __ldcg(cs.M_chain + c);
+    }
+}
 
 } // namespace csmc

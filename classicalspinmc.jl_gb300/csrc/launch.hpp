@@ -49,7 +49,7 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
 template <typename R>
 cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
                             const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem,
-                            const ResidentSel &sel, cudaStream_t st);
+                            const ResidentSel &sel, bool cooperative, cudaStream_t st);
 // CTAs (cl = 1) or clusters (cl > 1) of the selected resident kernel that fit on the device at once
 template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms);
 // static shared memory of the selected resident kernel in bytes (-1: query failed)

@@ -730,6 +730,21 @@ ClusterLayout make_cluster_layout(const Plan &P, int ranks) {
                     L.q2[((size_t)k * W + t) * L.Npl + i] = locate(P.p2[(size_t)t * P.Np + d], k);
             }
     }
+    // cubic and quartic partners, and the pattern of every local site
+    const int W3 = P.W3 * 2, W4 = P.W4 * 3;
+    L.q3.assign((size_t)ranks * std::max(W3, 1) * L.Npl, (uint16_t)sent_local);
+    L.q4.assign((size_t)ranks * std::max(W4, 1) * L.Npl, (uint16_t)sent_local);
+    L.pat.assign((size_t)ranks * L.Npl, (uint8_t)P.desc.nb);
+    for (int k = 0; k < ranks; k++)
+        for (int c = 0; c < C; c++)
+            for (int64_t j = 0; j < L.loc_count[k * C + c]; j++) {
+                const int64_t d = L.src_start[k * C + c] + j, i = L.loc_start[k * C + c] + j;
+                L.pat[(size_t)k * L.Npl + i] = P.pat[d];
+                for (int t = 0; t < W3; t++)
+                    L.q3[((size_t)k * W3 + t) * L.Npl + i] = locate(P.p3[(size_t)t * P.Np + d], k);
+                for (int t = 0; t < W4; t++)
+                    L.q4[((size_t)k * W4 + t) * L.Npl + i] = locate(P.p4[(size_t)t * P.Np + d], k);
+            }
     return L;
 }
 

@@ -85,7 +85,8 @@ Plan make_plan(const csmc_lattice_desc *d);
 // k holds part k of every colour class (parts of `part[c]` sites, a multiple
 // of 32, in device order), laid out class by class in its shared memory and
 // followed by a 32-site block of zeros (its sentinel).  Partners are encoded
-// (owner rank << 14) | owner-local index.
+// ((owner rank - reading rank) mod ranks) << 14 | owner-local index, so a
+// partner in the reading rank's own part has the top two bits clear.
 constexpr int CLUSTER_MAX = 4;
 struct ClusterLayout {
     int ranks = 1;
@@ -96,6 +97,11 @@ struct ClusterLayout {
     std::vector<int64_t> src_start;      // [rank][colour] device index of the part's first site
     // [rank][W2][Npl]: (owner rank - reading rank mod ranks) << 14 | owner-local index
     std::vector<uint16_t> q2;
+    // the same for the cubic and quartic partners: [rank][W3 * 2][Npl],
+    // [rank][W4 * 3][Npl]; and the basis of each local site, [rank][Npl]
+    // (padding: the padding pattern nb)
+    std::vector<uint16_t> q3, q4;
+    std::vector<uint8_t> pat;
 };
 // Throws csmc::Error if a rank would hold more than 16383 sites.
 ClusterLayout make_cluster_layout(const Plan &p, int ranks);

@@ -83,6 +83,38 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// Barrier across every CTA of a cooperative launch (all CTAs co-resident):
+// a monotonic arrival counter, zero at launch; the k-th barrier of the launch
+// completes when the counter reaches k * n_blocks.  Bounded: thread 0 gives
+// up after a fixed number of polls, or as soon as another CTA has reported an
+// error, and sets the error flag.  Returns false (block-uniform) on failure.
+__device__ __forceinline__ bool grid_barrier(unsigned int *ctr, unsigned int n_blocks, unsigned int &epoch,
+                                             int *error_flag, int *s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        epoch++;
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        const unsigned int target = epoch * n_blocks;
+        int ok = 0;
+        for (int k = 0; k < (1 << 22); k++) {
+            unsigned int v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+            if (v >= target) {
+                ok = 1;
+                break;
+            }
+            if ((k & 63) == 63 && *(volatile int *)error_flag) break;
+            __nanosleep(64);
+        }
+        if (!ok) atomicExch(error_flag, 1);
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
 // ---- thread-block cluster primitives
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -268,18 +300,38 @@ template <typename R, int CL> struct ResidentCommon {
             const int st = col_begin(col), n = col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const V3<R> s = sp.get(st + i);
-                const R n2 = s.x * s.x + s.y * s.y + s.z * s.z;
+                const R n2 = dot(s, s);
                 if (n2 == R(0)) continue;
-                const R f = S.S * Math<R>::rsqrt_(n2);
-                sp.set(st + i, {s.x * f, s.y * f, s.z * f});
+                using F = Fp<R>;
+                const R f = F::mul(S.S, Math<R>::rsqrt_(n2));
+                sp.set(st + i, {F::mul(s.x, f), F::mul(s.y, f), F::mul(s.z, f)});
             }
         }
         sy.bar();
     }
 };
 
+// Spins of a replica split over a cluster, as partner_fields sees them:
+// entry v = (relative owner << 14) | owner-local index; a partner in this
+// CTA's part (top bits clear) is a plain shared-memory load, one in another
+// rank's part a load through the shared::cluster window.  With CL = 1 the
+// entry is the local index itself.
+template <typename R, int CL> struct ClusterView {
+    Spins<R> sp;
+    uint32_t rb[CL]; // shared::cluster address of local site 0 of rank (rank + q) % CL, by q
+    uint32_t comp;   // double precision: bytes between the x, y and z blocks
+    __device__ __forceinline__ V3<R> get(int64_t v) const {
+        const uint32_t u = (uint32_t)v;
+        if (CL == 1 || (u >> 14) == 0u) return sp.get((int64_t)u);
+        const uint32_t q = u >> 14, local = u & 0x3FFFu;
+        uint32_t b = rb[0];
+        if (CL == 2) b = rb[1 % CL];
+        if (CL == 4) b = (q & 2u) ? ((q & 1u) ? rb[3 % CL] : rb[2 % CL]) : rb[1 % CL];
+        return cluster_spin(b + local * site_stride<R>(), comp, R(0));
+    }
+};
+
 template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : ResidentCommon<R, CL> {
-    static_assert(CL == 1, "the generic resident kernel runs one CTA per replica");
     static constexpr int kMaxThreads = 512; // 128 registers per thread
     static constexpr int kCoefSmem = 1;
     static constexpr bool kPartnerWords = false;
@@ -287,63 +339,75 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
     using B::c;
     using B::S;
     using B::sp;
+    Tab<uint16_t> tb;      // this rank's tables (local indices; CL = 1: the replica's)
+    ClusterView<R, CL> cv; // partner spins
     __device__ ResidentGeneric(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
                                const uint4 *, bool)
-        : B{s, sp_, sy_, c_, slot_, rk, coef} {}
+        : B{s, sp_, sy_, c_, slot_, rk, coef} {
+        tb = S.tb;
+        cv.sp = sp_;
+        cv.comp = (uint32_t)(S.Npl * sizeof(double));
+        if (CL > 1) {
+            const int64_t n = S.Npl;
+            tb.Np = n;
+            tb.p2 = S.q2c + (int64_t)rk * tb.W2 * n;
+            tb.p3 = S.q3c + (int64_t)rk * tb.W3 * 2 * n;
+            tb.p4 = S.q4c + (int64_t)rk * tb.W4 * 3 * n;
+            tb.pat = S.patc + (int64_t)rk * n;
+            const uint32_t a = smem_u32(spin_base(sp_));
+#pragma unroll
+            for (int q = 0; q < CL; q++) cv.rb[q] = map_rank(a, (uint32_t)((rk + q) % CL));
+        }
+    }
     __device__ void prepare() const {}
 
     __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
         unsigned acc = 0;
         for (int col = 0; col < S.n_colours; col++) {
-            const int st = (int)S.col_start[col], n = (int)S.col_count[col];
+            const int st = this->col_begin(col), n = this->col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                const int b = S.tb.pat[d];
+                const uint32_t dg = (uint32_t)this->device_index(col, d);
+                const int b = tb.pat[d];
                 V3<R> hb, hc, hq;
-                partner_fields<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, b, hb, hc, hq);
-                const R *h = S.cf.h + 3 * b;
-                const V3<R> hext = {hb.x + hc.x + hq.x - h[0], hb.y + hc.y + hq.y - h[1], hb.z + hc.z + hq.z - h[2]};
+                partner_fields<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, b, hb, hc, hq);
+                const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{S.cf.h[3 * b], S.cf.h[3 * b + 1], S.cf.h[3 * b + 2]});
                 const V3<R> s = sp.get(d);
-                const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1);
+                const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
                 const R dE = delta_e<R>(S.cf, b, s, sn, hext);
                 bool accept = dE < R(0);
-                if (!accept) {
-                    const R arg = sizeof(R) == 4 ? -dE * invT : -dE / (R)T;
-                    accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
-                }
+                if (!accept) accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
                 if (accept) {
                     sp.set(d, sn);
                     acc++;
                 }
             }
-            __syncthreads();
+            this->sy.bar();
         }
         return acc;
     }
 
     __device__ void or_sweep() const {
         for (int col = 0; col < S.n_colours; col++) {
-            const int st = (int)S.col_start[col], n = (int)S.col_count[col];
+            const int st = this->col_begin(col), n = this->col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, S.tb.pat[d]);
+                const V3<R> H = local_field<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, tb.pat[d]);
                 if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
-                const V3<R> s = sp.get(d);
-                const R proj = R(2) * dot(s, H) / (H.x * H.x + H.y * H.y + H.z * H.z);
-                sp.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
+                sp.set(d, reflect(sp.get(d), H, false));
             }
-            __syncthreads();
+            this->sy.bar();
         }
     }
 
     __device__ double energy() const { // valid in thread 0
         double e = 0.0;
         for (int col = 0; col < S.n_colours; col++) {
-            const int st = (int)S.col_start[col], n = (int)S.col_count[col];
+            const int st = this->col_begin(col), n = this->col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                e += site_energy_share<R, uint16_t, CUB, QUA>(S.tb, S.cf, sp, d, S.tb.pat[d]);
+                e += site_energy_share<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, tb.pat[d]);
             }
         }
         return this->sy.sum(e);
@@ -424,21 +488,13 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
 
     __device__ __forceinline__ V3<R> onsite(const R (&m)[9], V3<R> s) const {
         if (ONS == 0) return {R(0), R(0), R(0)};
-        if (ONS == 1) return {m[0] * s.x, m[4] * s.y, m[8] * s.z};
+        if (ONS == 1) return {Fp<R>::mul(m[0], s.x), Fp<R>::mul(m[4], s.y), Fp<R>::mul(m[8], s.z)};
         return matvec(m, s);
     }
 
     __device__ __forceinline__ void accumulate(V3<R> &hb, int col, int t, const R (&J)[W], V3<R> s) const {
-        if (BIL == 0) {
-            hb.x += J[t] * s.x;
-            hb.y += J[t] * s.y;
-            hb.z += J[t] * s.z;
-        } else {
-            const R *M = scoef + CSMC_MAX_COLOURS * kClassBlock + (col * W + t) * 9;
-            hb.x += M[0] * s.x + M[1] * s.y + M[2] * s.z;
-            hb.y += M[3] * s.x + M[4] * s.y + M[5] * s.z;
-            hb.z += M[6] * s.x + M[7] * s.y + M[8] * s.z;
-        }
+        if (BIL == 0) hb = add_scaled(hb, J[t], s);
+        else hb = add_matvec(hb, scoef + CSMC_MAX_COLOURS * kClassBlock + (col * W + t) * 9, s);
     }
 
     // the spin of cluster partner entry v = (relative owner q << 14) |
@@ -512,11 +568,9 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 wn = next_word(st, n, k);
                 const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
-                const V3<R> as = onsite(a, s);
-                const V3<R> H = {as.x + hb.x - h.x, as.y + hb.y - h.y, as.z + hb.z - h.z};
+                const V3<R> H = vsub(vadd(onsite(a, s), hb), h);
                 if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
-                const R proj = Math<R>::div_(R(2) * dot(s, H), H.x * H.x + H.y * H.y + H.z * H.z);
-                sp.set(d, {-s.x + proj * H.x, -s.y + proj * H.y, -s.z + proj * H.z});
+                sp.set(d, reflect(s, H, true));
             }
             this->sy.bar();
         }
@@ -537,16 +591,13 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 const uint32_t dg = (uint32_t)this->device_index(col, d);
                 const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
-                const V3<R> hext = {hb.x - h.x, hb.y - h.y, hb.z - h.z};
+                const V3<R> hext = vsub(hb, h);
                 const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
-                const V3<R> ds = {sn.x - s.x, sn.y - s.y, sn.z - s.z};
-                const R dE = (dot(sn, onsite(q, sn)) - dot(s, onsite(q, s))) + dot(ds, hext);
+                using F = Fp<R>;
+                const R dE = F::add(F::sub(dot(sn, onsite(q, sn)), dot(s, onsite(q, s))), dot(vsub(sn, s), hext));
                 bool accept = dE < R(0);
-                if (!accept) {
-                    const R arg = sizeof(R) == 4 ? -dE * invT : -dE / (R)T;
-                    accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(arg);
-                }
+                if (!accept) accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
                 if (accept) {
                     sp.set(d, sn);
                     acc++;
@@ -571,7 +622,8 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 wn = next_word(st, n, k);
                 const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
-                e += (double)(dot(s, onsite(m, s)) - dot(s, h)) + 0.5 * (double)dot(s, hb);
+                const double part = (double)Fp<R>::sub(dot(s, onsite(m, s)), dot(s, h));
+                e = Fp<double>::add(e, Fp<double>::fma(0.5, (double)dot(s, hb), part));
             }
         }
         return this->sy.sum(e);
@@ -598,6 +650,7 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ double scratch[32];
     __shared__ double red[4];
     __shared__ int s_item;
+    __shared__ int s_ok;
     __shared__ double s_sigma;
     __shared__ ResSys<R> s_sys;
     __shared__ R s_coef[K::kCoefSmem];
@@ -704,78 +757,111 @@ __global__ void __launch_bounds__(NT, 1)
             cluster_sync_all();
         }
 
-        const int slot = cs.slot_of[c];
-        const double T = rd.T_override > 0 ? rd.T_override : cs.T_slot[slot];
-        if (threadIdx.x == 0) s_sigma = rd.reset_sigma ? rd.sigma0 : cs.sigma_slot[slot];
-        __syncthreads();
-        const K k(S, sp, sync, c, slot, rank, s_coef, words ? swords : gwords, words);
+        const K k(S, sp, sync, c, 0, rank, s_coef, words ? swords : gwords, words);
         k.prepare();
-        const R invT = (R)(1.0 / T);
         const bool writer = threadIdx.x == 0 && rank == 0;
         double E = cs.E_chain[c];
-        double acc_total = 0.0;
         uint32_t msweep = rd.msweep0;
         // single precision: renormalise |s| = S whenever the context's total
         // sweep count passes a multiple of renorm_every
         uint64_t sweeps = rd.sweeps0;
         const uint64_t every = rd.renorm_every > 0 ? (uint64_t)rd.renorm_every : 0;
         uint64_t next_renorm = every ? (sweeps / every + 1) * every : 0;
+        unsigned int epoch = 0;
 
-        for (int64_t it = rd.it0; it < rd.it1; it++) {
-            if (rd.or_rate != 0) {
-                k.or_sweep();
-                sweeps++;
+        for (int64_t w0 = rd.it0; w0 < rd.it1;) {
+            // the window [w0, w1): the whole launch, or (persistent) up to the
+            // next exchange iteration.  The slot of this replica, its
+            // temperature and sigma are read per window: the exchange between
+            // windows moves replicas between slots (loads bypass L1, other
+            // blocks wrote them).
+            int64_t w1 = rd.it1;
+            if (rd.persistent && rd.swap_enabled) {
+                const int64_t q = (w0 + rd.swap_period - 1) / rd.swap_period * rd.swap_period;
+                if (q + 1 < w1) w1 = q + 1;
             }
-            const bool metro = it % dosweep == 0;
-            if (metro) {
-                const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
-                msweep++;
-                sweeps++;
-                const double at = sync.sum((double)a);
-                if (threadIdx.x == 0) {
-                    acc_total += at;
-                    if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) { // metropolis.jl:124-126
-                        const double om = 1 - at / (double)S.n_real;
-                        const double f = 0.5 / (om > 0.05 ? om : 0.05);
-                        double sg = s_sigma * f;
-                        s_sigma = sg < 0.0 ? 0.0 : (sg > 100 ? 100 : sg);
+            const int slot = __ldcg(cs.slot_of + c);
+            const double T = rd.T_override > 0 ? rd.T_override : __ldcg(cs.T_slot + slot);
+            if (threadIdx.x == 0)
+                s_sigma = (rd.reset_sigma && w0 == rd.it0) ? rd.sigma0 : __ldcg(cs.sigma_slot + slot);
+            __syncthreads();
+            const R invT = (R)(1.0 / T);
+            double acc_total = 0.0;
+
+            for (int64_t it = w0; it < w1; it++) {
+                if (rd.or_rate != 0) {
+                    k.or_sweep();
+                    sweeps++;
+                }
+                const bool metro = it % dosweep == 0;
+                if (metro) {
+                    const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
+                    msweep++;
+                    sweeps++;
+                    const double at = sync.sum((double)a);
+                    if (threadIdx.x == 0) {
+                        acc_total += at;
+                        if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) { // metropolis.jl:124-126
+                            const double om = 1 - at / (double)S.n_real;
+                            const double f = 0.5 / (om > 0.05 ? om : 0.05);
+                            double sg = s_sigma * f;
+                            s_sigma = sg < 0.0 ? 0.0 : (sg > 100 ? 100 : sg);
+                        }
+                    }
+                    __syncthreads();
+                    // energy needed: exchange point, a probe before the next
+                    // Metropolis sweep, or the last Metropolis sweep of the window
+                    bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
+                    for (int64_t q = it; q < it + dosweep && q < w1 && !needE; q++) needE = is_probe(rd, q);
+                    needE = needE || it + dosweep >= w1;
+                    if (needE) {
+                        const double e = k.energy();
+                        if (threadIdx.x == 0) E = e;
                     }
                 }
-                __syncthreads();
-                // energy needed: exchange point, a probe before the next
-                // Metropolis sweep, or the last Metropolis sweep of the window
-                bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-                for (int64_t q = it; q < it + dosweep && q < rd.it1 && !needE; q++) needE = is_probe(rd, q);
-                needE = needE || it + dosweep >= rd.it1;
-                if (needE) {
-                    const double e = k.energy();
-                    if (threadIdx.x == 0) E = e;
-                }
-            }
-            // a probe at an exchange iteration (the window's last) is recorded
-            // by the exchange kernel after the exchange, from M_chain
-            const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-            if (is_probe(rd, it)) {
-                const double M = k.magnetization();
-                if (writer) {
-                    const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
-                    if (!swap_here && kq >= 0 && kq < rd.probe_cap) {
-                        if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
-                        if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
+                // a probe at an exchange iteration (the window's last) is
+                // recorded after the exchange, from M_chain
+                const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
+                if (is_probe(rd, it)) {
+                    const double M = k.magnetization();
+                    if (writer) {
+                        const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
+                        if (!swap_here && kq >= 0 && kq < rd.probe_cap) {
+                            if (rd.rec_E) rd.rec_E[kq * rd.n_slots + slot] = E;
+                            if (rd.rec_M) rd.rec_M[kq * rd.n_slots + slot] = M;
+                        }
+                        cs.M_chain[c] = M;
                     }
-                    cs.M_chain[c] = M;
+                }
+                if (sizeof(R) == 4 && every && sweeps >= next_renorm) {
+                    k.renormalize();
+                    next_renorm = (sweeps / every + 1) * every;
                 }
             }
-            if (sizeof(R) == 4 && every && sweeps >= next_renorm) {
-                k.renormalize();
-                next_renorm = (sweeps / every + 1) * every;
-            }
-        }
 
-        if (writer) {
-            cs.E_chain[c] = E;
-            cs.acc_slot[slot] += acc_total;
-            cs.sigma_slot[slot] = s_sigma;
+            if (writer) {
+                cs.E_chain[c] = E;
+                cs.acc_slot[slot] = __ldcg(cs.acc_slot + slot) + acc_total;
+                cs.sigma_slot[slot] = s_sigma;
+            }
+            const int64_t last = w1 - 1;
+            w0 = w1;
+            if (!rd.persistent || !rd.swap_enabled || last % rd.swap_period != 0) break;
+            // exchange of every lattice by block 0 between two grid barriers,
+            // then the probe record of the exchange iteration
+            if (!grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok)) break;
+            if (blockIdx.x == 0) {
+                for (int L = 0; L < rd.n_lattices; L++)
+                    exchange_slots(cs, L, rd.lattices[L].x, rd.lattices[L].y, last, rd.swap_rate, rd.k0, rd.k1);
+                if (is_probe(rd, last)) {
+                    const int64_t kq = (last - rd.probe_first) / rd.probe_rate;
+                    __syncthreads();
+                    if (kq >= 0 && kq < rd.probe_cap)
+                        for (int L = 0; L < rd.n_lattices; L++)
+                            record_slots(cs, rd.lattices[L].x, rd.lattices[L].y, rd.rec_E, rd.rec_M, kq, rd.n_slots);
+                }
+            }
+            if (!grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok)) break;
         }
         // every thread's shared-memory accesses are ordered before the bulk
         // copies that follow (the stores below, the next item's staging)
@@ -815,7 +901,14 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 // Kernel entry points of each instantiation family (resident_*.cu).
-template <typename R> const void *resident_kernel_generic(bool cub, bool qua);
+template <typename R> const void *resident_kernel_generic(bool cub, bool qua, int cl);
+
+template <typename R, bool CUB, bool QUA> const void *resident_generic_for(int cl) {
+    constexpr int NT = resident_max_threads(false, 0, 0);
+    if (cl == 4) return (const void *)k_resident<ResidentGeneric<R, CUB, QUA, 4>, R, NT, 4>;
+    if (cl == 2) return (const void *)k_resident<ResidentGeneric<R, CUB, QUA, 2>, R, NT, 2>;
+    return (const void *)k_resident<ResidentGeneric<R, CUB, QUA, 1>, R, NT, 1>;
+}
 // specialised kernels of width W (defined in resident_fast_<precision>_w<W>.cu)
 template <typename R, int W> const void *resident_kernel_fast(int bil, int ons, int cl);
 

@@ -1,20 +1,12 @@
-// resident_generic.cu -- instantiations of the generic resident kernel and the
-// host launcher that picks a resident kernel (resident.cuh).
+// resident_generic.cu -- the host launcher that picks a resident kernel
+// (resident.cuh) and queries its occupancy and shared memory.
 #include "launch.hpp"
 #include "resident.cuh"
 
 namespace csmc {
 
-template <typename R> const void *resident_kernel_generic(bool cub, bool qua) {
-    constexpr int NT = resident_max_threads(false, 0, 0);
-    if (cub && qua) return (const void *)k_resident<ResidentGeneric<R, true, true, 1>, R, NT, 1>;
-    if (cub) return (const void *)k_resident<ResidentGeneric<R, true, false, 1>, R, NT, 1>;
-    if (qua) return (const void *)k_resident<ResidentGeneric<R, false, true, 1>, R, NT, 1>;
-    return (const void *)k_resident<ResidentGeneric<R, false, false, 1>, R, NT, 1>;
-}
-
 template <typename R> static const void *pick(const ResidentSel &sel) {
-    if (!sel.fast) return resident_kernel_generic<R>(sel.cub, sel.qua);
+    if (!sel.fast) return resident_kernel_generic<R>(sel.cub, sel.qua, sel.cl);
     if (sel.width <= 4) return resident_kernel_fast<R, 4>(sel.bil, sel.ons, sel.cl);
     if (sel.width <= 6) return resident_kernel_fast<R, 6>(sel.bil, sel.ons, sel.cl);
     return resident_kernel_fast<R, 8>(sel.bil, sel.ons, sel.cl);
@@ -23,7 +15,7 @@ template <typename R> static const void *pick(const ResidentSel &sel) {
 template <typename R>
 cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_items, int *work_ctr,
                             const ChainState &cs, const RunDesc &rd, int grid, int block, size_t smem,
-                            const ResidentSel &sel, cudaStream_t st) {
+                            const ResidentSel &sel, bool cooperative, cudaStream_t st) {
     // work_ctr must be zero when the kernel starts (the caller resets it on `st`)
     if (block < 32 || block > resident_max_threads(sel.fast, sel.bil, sel.ons) || block % 32 != 0)
         return cudaErrorInvalidValue;
@@ -33,19 +25,30 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
     ChainState csv = cs;
     RunDesc rdv = rd;
     void *args[] = {(void *)&d_sys, (void *)&items, (void *)&n_items, (void *)&work_ctr, (void *)&csv, (void *)&rdv};
-    if (sel.cl <= 1) return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st);
+    if (sel.cl <= 1 && !cooperative) return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st);
+    // clusters and/or a cooperative launch (every CTA co-resident, for the
+    // persistent kernel's grid barriers)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = sel.cl;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
+    cudaLaunchAttribute attr[2];
+    int na = 0;
+    if (sel.cl > 1) {
+        attr[na].id = cudaLaunchAttributeClusterDimension;
+        attr[na].val.clusterDim.x = sel.cl;
+        attr[na].val.clusterDim.y = 1;
+        attr[na].val.clusterDim.z = 1;
+        na++;
+    }
+    if (cooperative) {
+        attr[na].id = cudaLaunchAttributeCooperative;
+        attr[na].val.cooperative = 1;
+        na++;
+    }
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = na;
     return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
@@ -82,12 +85,11 @@ template <typename R> int resident_static_smem(const ResidentSel &sel) {
     return (int)at.sharedSizeBytes;
 }
 
-template const void *resident_kernel_generic<float>(bool, bool);
-template const void *resident_kernel_generic<double>(bool, bool);
 template cudaError_t launch_resident<float>(const ResSys<float> *, const int2 *, int, int *, const ChainState &,
-                                            const RunDesc &, int, int, size_t, const ResidentSel &, cudaStream_t);
+                                            const RunDesc &, int, int, size_t, const ResidentSel &, bool, cudaStream_t);
 template cudaError_t launch_resident<double>(const ResSys<double> *, const int2 *, int, int *, const ChainState &,
-                                             const RunDesc &, int, int, size_t, const ResidentSel &, cudaStream_t);
+                                             const RunDesc &, int, int, size_t, const ResidentSel &, bool,
+                                             cudaStream_t);
 template int resident_capacity<float>(int, size_t, const ResidentSel &, int);
 template int resident_capacity<double>(int, size_t, const ResidentSel &, int);
 template int resident_static_smem<float>(const ResidentSel &);

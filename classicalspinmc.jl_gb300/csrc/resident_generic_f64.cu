@@ -1,0 +1,15 @@
+// resident_generic_f64.cu -- instantiations of the generic resident kernel (resident.cuh) in
+// double precision: with and without cubic / quartic terms, one CTA per
+// replica or a cluster of 2 or 4.
+#include "resident.cuh"
+
+namespace csmc {
+
+template <> const void *resident_kernel_generic<double>(bool cub, bool qua, int cl) {
+    if (cub && qua) return resident_generic_for<double, true, true>(cl);
+    if (cub) return resident_generic_for<double, true, false>(cl);
+    if (qua) return resident_generic_for<double, false, true>(cl);
+    return resident_generic_for<double, false, false>(cl);
+}
+
+} // namespace csmc

@@ -406,11 +406,11 @@ def autotune(mc: MonteCarlo, n_windows: int = 4, alg: _Alg | None = None) -> lis
     rp.probe_rate = p.probe_rate
     rp.kind = alg.kind
     rp.path = _PATHS[mc.path]
-    entries = (_lib.TuneEntry * 8)()
+    entries = (_lib.TuneEntry * 16)()
     n = C.c_int32()
-    mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, 8, C.byref(n))
-    return [{"cluster": e.cluster, "block": e.block, "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)}
-            for e in entries[:n.value]]
+    mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, 16, C.byref(n))
+    return [{"cluster": e.cluster, "block": e.block, "persistent": bool(e.persistent),
+             "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)} for e in entries[:n.value]]
 
 
 def _print_runtime_statistics(mc, t, acc, exc, n):

@@ -265,10 +265,23 @@ int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_therm
 int csmc_set_cluster_size(void *ctx, int32_t ranks);
 int csmc_cluster_size(void *ctx, int32_t *ranks);
 
+/* Persistent exchange windows (a tuning knob of this library; no counterpart
+ * in the reference).  On (the default): when every replica of the context is
+ * resident on the device at once, csmc_run runs up to 128 exchange windows in
+ * one cooperative launch of the resident kernel, whose blocks meet at a
+ * bounded grid barrier after each window while block 0 performs the replica
+ * exchange and the probe record; the replicas stay in shared memory across
+ * windows.  Off, or if the device refuses the cooperative launch: one launch
+ * per window and a separate exchange launch.  Both give the same chain.
+ * csmc_persistent reports whether persistent launches are in use. */
+int csmc_set_persistent(void *ctx, int32_t on);
+int csmc_persistent(void *ctx, int32_t *on);
+
 /* Autotuner of the resident kernel's launch configuration (no counterpart in
  * the reference; the tuning knobs are this library's).  For every cluster size
- * that fits (1, 2 or 4 CTAs per replica) and two block sizes (the balanced one
- * and the kernel's largest), it times n_windows exchange windows of the
+ * that fits (1, 2 or 4 CTAs per replica), two block sizes (the balanced one
+ * and the kernel's largest) and persistent windows on and off (see
+ * csmc_set_persistent), it times n_windows exchange windows of the
  * schedule in *params on the context's own replicas, restores the replicas and
  * every counter exactly (the chain continues as if no tuning had happened),
  * and keeps the fastest configuration for later runs.  entries[capacity]
@@ -277,6 +290,7 @@ int csmc_cluster_size(void *ctx, int32_t *ranks);
 typedef struct {
     int32_t cluster;       /* CTAs per replica */
     int32_t block;         /* threads per CTA */
+    int32_t persistent;    /* 1: windows and exchanges in one cooperative launch */
     double ms_per_window;  /* device time of one exchange window */
     int32_t chosen;        /* 1 for the configuration kept */
 } csmc_tune_entry;

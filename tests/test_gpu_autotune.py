@@ -52,3 +52,30 @@ def test_autotune_on_the_global_path_is_a_no_op(m, orc):
     before = mc.spins(1).copy()
     assert m.autotune(mc, n_windows=1) == []
     assert np.array_equal(mc.spins(1), before)
+
+
+def _set_persistent(mc, on):
+    import ctypes as C
+    mc.ctx.call("csmc_set_persistent", 1 if on else 0)
+    got = C.c_int32()
+    mc.ctx.call("csmc_persistent", C.byref(got))
+    return got.value
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["sc", "honeycomb", "triangular_open", "pyrochlore"])
+def test_persistent_windows_equal_one_launch_per_window(m, orc, name, precision):
+    """Exchange windows in one cooperative launch (grid barriers, exchange by
+    block 0) give the same chain, records and counters as one launch per
+    window with a separate exchange launch."""
+    res = []
+    for on in (False, True):
+        lat, _, mc = setup(m, orc, name, precision, R=4, seed=9)
+        assert _set_persistent(mc, on) in ((0,) if not on else (0, 1))
+        res.append(_pt(m, mc, lat, tune=False)[1])
+    ref, got = res
+    assert np.abs(ref[0] - got[0]).max() <= 1e-12 * (1 if precision == "fp64" else 1e6)
+    assert np.abs(ref[1] - got[1]).max() <= 1e-9 * lat.size
+    assert np.abs(ref[2] - got[2]).max() <= 1e-9 * lat.size
+    assert np.array_equal(ref[3], got[3]) and np.array_equal(ref[4], got[4])
+    assert np.allclose(ref[5], got[5], rtol=1e-12)

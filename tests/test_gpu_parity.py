@@ -444,11 +444,13 @@ def _cluster(mc, ranks=None):
 
 
 @pytest.mark.parametrize("ranks", [2, 4])
-@pytest.mark.parametrize("name", ["square", "honeycomb", "sc", "sc24", "triangular_open", "asym_open", "selfloop"])
+@pytest.mark.parametrize("name", ["square", "honeycomb", "sc", "sc24", "triangular_open", "asym_open", "selfloop",
+                                  "pyrochlore"])
 def test_cluster_resident_single_sweeps_match_oracle(m, orc, name, ranks):
     """The resident kernel split over a cluster of 2 or 4 CTAs (partners of
     other ranks read through distributed shared memory) == the oracle, one
-    overrelaxation and one Metropolis sweep in colour order, FP64."""
+    overrelaxation and one Metropolis sweep in colour order, FP64.  The
+    pyrochlore with cubic and quartic terms runs the generic kernel."""
     seed = 23
     lat, ol, mc = setup(m, orc, name, "fp64", seed=seed, T=0.6)
     assert _cluster(mc, ranks) == ranks
@@ -465,7 +467,7 @@ def test_cluster_resident_single_sweeps_match_oracle(m, orc, name, ranks):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("name", ["sc", "honeycomb", "triangular_open"])
+@pytest.mark.parametrize("name", ["sc", "honeycomb", "triangular_open", "pyrochlore"])
 def test_cluster_sizes_give_the_same_chain(m, orc, name, precision):
     """One CTA per replica and clusters of 2 and 4 CTAs run the same
     arithmetic per site: a parallel-tempering window with exchanges, probes and
