@@ -215,10 +215,20 @@ def bench_ours(args, rank, world, dist):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("k_resident_fp32_sc_L24_R64")
+    # the level that binds: the replicas stay in shared memory, so the same
+    # algorithmic bytes are also set against the nominal shared-memory
+    # bandwidth of the SMs in use (128 B per clock per SM)
+    sm_mhz = (clk.summary().get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0))
+    smem_peak = 152 * 128 * sm_mhz * 1e6 / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                        "traffic": traffic, "kernel": "k_resident<float>",
                        "kernel_ms_per_launch": per_launch_s * 1e3, "algorithmic_bytes_per_launch": bytes_per_launch,
-                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"}
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+                       "note": "replicas resident in shared memory for whole launches: achieved is the algorithmic "
+                               "96 B per update over the kernel time (the HBM rate a streaming kernel would need); "
+                               "traffic is the DRAM bytes of one launch (staging), measured by ncu",
+                       "on_chip": {"level": "shared memory", "achieved": achieved, "nominal_peak": smem_peak,
+                                   "unit": "GB/s", "frac": achieved / smem_peak}}
 
     # end to end through the C ABI with host buffers
     nh = R_REPL * lat.size * 3

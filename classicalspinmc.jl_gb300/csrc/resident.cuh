@@ -6,7 +6,10 @@
 // it is staged in with bulk TMA copies (cp.async.bulk, completion on an
 // mbarrier, bounded wait), updated colour class by colour class with a
 // barrier between classes, and written back once (single precision: bulk
-// TMA stores).
+// TMA stores).  A persistent launch (cooperative, every replica resident)
+// runs many exchange windows: the replicas stay in shared memory, and between
+// windows all CTAs meet at a bounded grid barrier while block 0 performs the
+// replica exchange (monte_carlo.jl:308-349) and the probe record.
 //
 // Shared-memory layout: the replica's spins in the device layout (single
 // precision: one float4 per site; double: x | y | z blocks), then, for the
