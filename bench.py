@@ -164,7 +164,8 @@ def bench_ours(args, rank, world, dist):
         entries = (L.TuneEntry * 16)()
         n = C.c_int32()
         ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 16, C.byref(n))
-        tuned = [{"cluster": e.cluster, "block": e.block, "persistent": bool(e.persistent),
+        tuned = [{"path": "global" if e.path == L.PATH_GLOBAL else "resident", "cluster": e.cluster,
+                  "block": e.block, "persistent": bool(e.persistent),
                   "ms_per_window": round(e.ms_per_window, 5), "chosen": bool(e.chosen)} for e in entries[:n.value]]
     ranks = C.c_int32()
     ctx.call("csmc_cluster_size", C.byref(ranks))
@@ -354,6 +355,18 @@ def bench_other(args):
         upd = sites * (iters + iters // kw["or_rate"])
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     it = [1]
+    tuned = []
+    if not args.no_autotune:  # resident configuration or global sweeps, timed on these replicas
+        rp = L.RunParams()
+        rp.sweep_start, rp.n_sweeps, rp.t_thermalization = 1, 0, 0
+        rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = kw["or_rate"], kw["swap_rate"], kw["probe_rate"]
+        rp.kind, rp.path = L.METROPOLIS, L.PATH_AUTO
+        entries = (L.TuneEntry * 16)()
+        n = C.c_int32()
+        ctx.call("csmc_autotune", C.byref(rp), 4, entries, 16, C.byref(n))
+        tuned = [{"path": "global" if e.path == L.PATH_GLOBAL else "resident", "cluster": e.cluster,
+                  "block": e.block, "persistent": bool(e.persistent), "ms_per_window": round(e.ms_per_window, 5),
+                  "chosen": bool(e.chosen)} for e in entries[:n.value]]
 
     def step():
         if anneal:
@@ -389,7 +402,8 @@ def bench_other(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
             "config": {"workload": args.workload, "description": desc, "site_updates_per_step": upd,
-                       "ctas_per_replica": cl.value, "l2": "flushed between steps (256 MB write)"},
+                       "ctas_per_replica": cl.value, "l2": "flushed between steps (256 MB write)",
+                       "autotune_candidates": tuned},
             "clocks": clk.summary(), "gpu_launches": launches}
     print(json.dumps(line))
 

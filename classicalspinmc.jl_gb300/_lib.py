@@ -64,7 +64,7 @@ class RunParams(C.Structure):
 
 
 class TuneEntry(C.Structure):
-    _fields_ = [("cluster", C.c_int32), ("block", C.c_int32), ("persistent", C.c_int32),
+    _fields_ = [("path", C.c_int32), ("cluster", C.c_int32), ("block", C.c_int32), ("persistent", C.c_int32),
                 ("ms_per_window", C.c_double), ("chosen", C.c_int32)]
 
 

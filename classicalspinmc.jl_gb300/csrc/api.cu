@@ -112,6 +112,7 @@ struct Ctx {
     int n_items = 0;
     int cl = 1;         // CTAs per replica of the resident kernel
     int block_pref = 0; // threads per CTA chosen by csmc_autotune (0: automatic)
+    bool global_pref = false; // csmc_autotune found the global path faster for CSMC_PATH_AUTO runs
     uint32_t msweep = 0;   // Metropolis sweeps so far (the Philox counter)
     uint64_t nsweeps = 0;  // sweeps of every kind so far (renormalisation cadence)
     int renorm_every = 64;
@@ -786,7 +787,7 @@ static int choose_path(Ctx &C, int requested) {
                 "and at most 65536 padded sites");
         return CSMC_PATH_RESIDENT;
     }
-    return all ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
+    return all && !C.global_pref ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
 }
 
 // Threads per CTA of the resident kernel.  `hint` (a multiple of 32) forces a
@@ -1624,7 +1625,17 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
                      int *n_out) {
     require(p != nullptr && n_windows >= 1, CSMC_ERR_INVALID, "autotune needs run parameters and n_windows >= 1");
     *n_out = 0;
-    if (choose_path(C, p->path) != CSMC_PATH_RESIDENT) return; // nothing to tune: the run takes the global path
+    // a run that asks for the global path has nothing to tune; an automatic
+    // run also times the global path against the resident configurations
+    if (p->path == CSMC_PATH_GLOBAL || p->path == CSMC_PATH_PER_REPLICA) return;
+    C.global_pref = false;
+    bool resident = true;
+    for (auto &S : C.sys) resident = resident && S->resident_ok;
+    if (!resident && p->path == CSMC_PATH_AUTO) {
+        C.global_pref = false;
+        return; // the global path is the only one
+    }
+    require(resident, CSMC_ERR_UNSUPPORTED, "resident path requested but the lattices do not fit it");
     csmc_run_params q = *p;
     q.path = CSMC_PATH_RESIDENT;
     q.resident_block = 0;
@@ -1639,6 +1650,7 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
         int cl, block;
         bool persistent;
         double ms;
+        bool global = false;
     };
     std::vector<Cand> cands;
     for (int cl : {1, 2, 4}) {
@@ -1670,14 +1682,30 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
         }
     }
     require(!cands.empty(), CSMC_ERR_UNSUPPORTED, "no resident configuration fits these lattices");
+    if (p->path == CSMC_PATH_AUTO) { // the global colour sweeps as one more candidate
+        csmc_run_params g = q;
+        g.path = CSMC_PATH_GLOBAL;
+        run(C, &g);
+        saved.restore(C);
+        run(C, &g);
+        Cand cg{0, 0, false, C.last_ms / n_windows};
+        cg.global = true;
+        cands.push_back(cg);
+        saved.restore(C);
+    }
     size_t best = 0;
     for (size_t k = 1; k < cands.size(); k++)
         if (cands[k].ms < cands[best].ms) best = k;
-    choose_cluster(C, cands[best].cl);
+    size_t best_res = cands[best].global ? 0 : best; // resident configuration kept for explicit requests
+    for (size_t k = 0; k < cands.size(); k++)
+        if (!cands[k].global && cands[k].ms < cands[best_res].ms) best_res = k;
+    choose_cluster(C, cands[best_res].cl);
     upload_resident(C);
-    C.block_pref = cands[best].block;
-    C.persistent_on = cands[best].persistent;
+    C.block_pref = cands[best_res].block;
+    C.persistent_on = cands[best_res].persistent;
+    C.global_pref = cands[best].global;
     for (size_t k = 0; k < cands.size() && (int)k < capacity; k++) {
+        out[k].path = cands[k].global ? CSMC_PATH_GLOBAL : CSMC_PATH_RESIDENT;
         out[k].cluster = cands[k].cl;
         out[k].block = cands[k].block;
         out[k].persistent = cands[k].persistent ? 1 : 0;

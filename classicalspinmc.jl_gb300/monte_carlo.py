@@ -409,7 +409,9 @@ def autotune(mc: MonteCarlo, n_windows: int = 4, alg: _Alg | None = None) -> lis
     entries = (_lib.TuneEntry * 16)()
     n = C.c_int32()
     mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, 16, C.byref(n))
-    return [{"cluster": e.cluster, "block": e.block, "persistent": bool(e.persistent),
+    paths = {_lib.PATH_RESIDENT: "resident", _lib.PATH_GLOBAL: "global"}
+    return [{"path": paths.get(e.path, "resident"), "cluster": e.cluster, "block": e.block,
+             "persistent": bool(e.persistent),
              "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)} for e in entries[:n.value]]
 
 

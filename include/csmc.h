@@ -277,18 +277,21 @@ int csmc_cluster_size(void *ctx, int32_t *ranks);
 int csmc_set_persistent(void *ctx, int32_t on);
 int csmc_persistent(void *ctx, int32_t *on);
 
-/* Autotuner of the resident kernel's launch configuration (no counterpart in
- * the reference; the tuning knobs are this library's).  For every cluster size
- * that fits (1, 2 or 4 CTAs per replica), two block sizes (the balanced one
- * and the kernel's largest) and persistent windows on and off (see
- * csmc_set_persistent), it times n_windows exchange windows of the
+/* Autotuner of the launch configuration (no counterpart in the reference; the
+ * tuning knobs are this library's).  For every cluster size that fits (1, 2
+ * or 4 CTAs per replica), two block sizes (the balanced one and the resident
+ * kernel's largest), persistent windows on and off (see csmc_set_persistent)
+ * and, when params->path is CSMC_PATH_AUTO, the global colour-sweep path, it
+ * times n_windows exchange windows of the
  * schedule in *params on the context's own replicas, restores the replicas and
  * every counter exactly (the chain continues as if no tuning had happened),
- * and keeps the fastest configuration for later runs.  entries[capacity]
+ * and keeps the fastest configuration for later CSMC_PATH_AUTO runs (the
+ * fastest resident configuration for CSMC_PATH_RESIDENT runs).  entries[capacity]
  * receives the candidates with their device time per window; n_entries the
  * number of candidates (0 when the lattices run on the global path). */
 typedef struct {
-    int32_t cluster;       /* CTAs per replica */
+    int32_t path;          /* CSMC_PATH_RESIDENT or CSMC_PATH_GLOBAL */
+    int32_t cluster;       /* CTAs per replica (resident) */
     int32_t block;         /* threads per CTA */
     int32_t persistent;    /* 1: windows and exchanges in one cooperative launch */
     double ms_per_window;  /* device time of one exchange window */

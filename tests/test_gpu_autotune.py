@@ -79,3 +79,22 @@ def test_persistent_windows_equal_one_launch_per_window(m, orc, name, precision)
     assert np.abs(ref[2] - got[2]).max() <= 1e-9 * lat.size
     assert np.array_equal(ref[3], got[3]) and np.array_equal(ref[4], got[4])
     assert np.allclose(ref[5], got[5], rtol=1e-12)
+
+
+def test_autotune_automatic_path_also_times_the_global_sweeps(m, orc):
+    """With the automatic path the global colour sweeps are one more
+    candidate; whichever is kept, the chain runs on and its energies match
+    the oracle's total energy of the final spins."""
+    lat, ol, mc = setup(m, orc, "pyrochlore", "fp32", R=2, seed=3)
+    mc.path = "auto"
+    mc.ctx.set_temperatures(np.array([0.3, 0.9]))
+    entries = m.autotune(mc, n_windows=2)
+    assert any(e["path"] == "global" for e in entries) and any(e["path"] == "resident" for e in entries)
+    assert sum(e["chosen"] for e in entries) == 1
+    p = mc.parameters
+    p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 0, 20, 20, 10
+    p.probe_rate, p.swap_rate, p.overrelaxation_rate = 5, 5, 5
+    m.parallel_tempering(mc, verbose=False)
+    for r in range(2):
+        s = mc.spins(r)
+        assert abs(m.total_energy(mc, r) - ol.total_energy(np.asfortranarray(s))) <= 1e-4 * lat.size
