@@ -408,6 +408,41 @@ def bench_other(args):
     print(json.dumps(line))
 
 
+def bench_structure_factor(args):
+    """compute_equal_time_correlations of all 64 replicas of the simple-cubic
+    L=24 workload at every allowed wavevector 2 pi n / L (13824 k-points),
+    FP32: site-phase products (k-points x sites x replicas) per second of
+    device time."""
+    import torch
+    m = G.load()
+    torch.cuda.set_device(0)
+    lat = make_lattice(m)
+    mc = m.MonteCarlo(list(temperatures()), lat, {}, precision="fp32", seed=SEED)
+    mc.ctx.call("csmc_random_spins", C.c_uint64(SEED))
+    n = np.stack(np.unravel_index(np.arange(L_SIDE ** 3), (L_SIDE,) * 3), axis=0)
+    ks = np.asfortranarray(2 * np.pi * n / L_SIDE, dtype=np.float64)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        m.structure_factors(mc, ks)
+    t = 0.0
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            m.structure_factors(mc, ks)
+            t += stats(mc.ctx)[0] / 1e3
+    products = ks.shape[1] * lat.size * R_REPL
+    line = {"metric": "structure factor: k-point x site x replica products per second", "value": products * args.steps / t,
+            "unit": "products/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "structure_factor", "lattice": "simple cubic L=24 (13824 sites)",
+                       "replicas": R_REPL, "k_points": int(ks.shape[1]),
+                       "fp32_fma_per_product": 6, "l2": "flushed between steps (256 MB write)"},
+            "clocks": clk.summary(), "gpu_launches": args.steps}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,10 +459,13 @@ def main():
                     help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",
                     choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
-                             "pyrochlore_large_fp32"],
+                             "pyrochlore_large_fp32", "structure_factor"],
                     help="sc_pt (default): the 64-replica simple-cubic line; the others measure the remaining "
                          "configurations (device throughput only)")
     args = ap.parse_args()
+    if args.workload == "structure_factor":
+        bench_structure_factor(args)
+        return
     if args.workload != "sc_pt":
         bench_other(args)
         return

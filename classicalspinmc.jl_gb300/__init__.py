@@ -14,7 +14,8 @@ from .lattice import Lattice, get_spin, random_spin_orientation, set_spin  # noq
 from .monte_carlo import (MCParamsBuffer, Metropolis, MetropolisAdaptive, MetropolisFixedCone,  # noqa: F401
                           MonteCarlo, SimulationParameters, annealing_temperatures, deterministic_updates,
                           energy_density, get_local_field, get_magnetization, local_fields, overrelaxation,
-                          parallel_tempering, replay, simulated_annealing, total_energy, autotune)
+                          parallel_tempering, replay, simulated_annealing, total_energy, autotune,
+                          compute_equal_time_correlations, structure_factors)
 from . import examples  # noqa: F401
 from .observables import specific_heat, susceptibility  # noqa: F401
 from .unit_cell import (FCC, BreathingPyrochlore, Honeycomb, Pyrochlore, Square, Triangular,  # noqa: F401

@@ -1154,6 +1154,36 @@ static void anneal(Ctx &C, const double *temps, int n_temps, int64_t t_therm, in
     C.last_launches = L.n;
 }
 
+// compute_equal_time_correlations of every replica of one lattice (csmc_structure_factor)
+template <typename R>
+static void structure_factor(Ctx &C, System &S, const SysArgs<R> &a, int dim, const double *positions, int64_t n_k,
+                             const double *ks, double *Suv) {
+    const Plan &P = S.plan;
+    std::vector<R> pd((size_t)P.Np * 3, R(0)), kd((size_t)std::max<int64_t>(n_k, 1) * 3, R(0));
+    for (int64_t d = 0; d < P.Np; d++) {
+        const int64_t i = P.dev2ref[d];
+        if (i < 0) continue;
+        for (int x = 0; x < dim; x++) pd[(size_t)d * 3 + x] = (R)positions[(size_t)i * dim + x];
+    }
+    for (int64_t n = 0; n < n_k; n++)
+        for (int x = 0; x < dim; x++) kd[(size_t)n * 3 + x] = (R)ks[(size_t)n * dim + x];
+    DevBuf<R> dpos, dks;
+    DevBuf<double> dout;
+    dpos.upload(pd);
+    dks.upload(kd);
+    dout.alloc((size_t)S.R * std::max<int64_t>(n_k, 1) * 9);
+    C.reset_kernel_time();
+    auto ev = C.next_kernel_events();
+    CK(cudaEventRecord(ev.first, C.st));
+    launch_structure_factor<R>(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, C.st);
+    CK(cudaEventRecord(ev.second, C.st));
+    sync_check(C);
+    C.collect_kernel_time();
+    C.last_ms = C.last_kernel_ms;
+    C.last_launches = 1;
+    if (n_k > 0) CK(cudaMemcpy(Suv, dout.p, (size_t)S.R * n_k * 9 * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
 static void ensure_exact(Ctx &C, System &S) {
     if (S.exact_ready) return;
     const Plan &P = S.plan;
@@ -1726,6 +1756,33 @@ int csmc_autotune(void *c, const csmc_run_params *params, int32_t n_windows, csm
     CK(cudaStreamSynchronize(C.st));
     autotune(C, params, n_windows, entries, capacity, &n);
     *n_entries = n;
+    API_END
+}
+
+
+int csmc_structure_factor(void *c, int32_t lattice, int32_t dim, const double *positions, int64_t n_k,
+                          const double *ks, double *Suv) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(lattice >= 0 && lattice < (int)C.sys.size(), CSMC_ERR_INVALID, "bad lattice index");
+    require(dim >= 1 && dim <= 3, CSMC_ERR_INVALID, "dim must be 1, 2 or 3");
+    require(n_k >= 0 && (n_k == 0 || (positions && ks && Suv)), CSMC_ERR_INVALID, "positions, ks or Suv missing");
+    System &S = *C.sys[lattice];
+    CK(cudaStreamSynchronize(C.st));
+    if (C.precision == CSMC_FP32) structure_factor<float>(C, S, S.fa, dim, positions, n_k, ks, Suv);
+    else structure_factor<double>(C, S, S.da, dim, positions, n_k, ks, Suv);
+    API_END
+}
+
+int csmc_selftest_timeout(void *c, int32_t which) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(which == 0 || which == 1, CSMC_ERR_INVALID, "which must be 0 (mbarrier) or 1 (grid barrier)");
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaMemsetAsync(C.grid_bar.p, 0, sizeof(unsigned int), C.st));
+    CK(launch_wait_selftest(which, C.grid_bar.p, C.error_flag.p, C.st));
+    sync_check(C); // throws CSMC_ERR_TIMEOUT when the wait gave up, as it must
+    throw Error(CSMC_ERR_INVALID, "self-test: a wait that cannot complete reported success");
     API_END
 }
 

@@ -52,6 +52,13 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
                             const ResidentSel &sel, bool cooperative, cudaStream_t st);
 // CTAs (cl = 1) or clusters (cl > 1) of the selected resident kernel that fit on the device at once
 template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms);
+// compute_equal_time_correlations of every replica of one lattice (correlations.cu):
+// pos 3 per device site, ks 3 per wavevector, out [slot - slot_base][n_k][9]
+template <typename R>
+void launch_structure_factor(const SysArgs<R> &a, const R *pos, const R *ks, int64_t n_k, const int32_t *slot_of,
+                             int slot_base, double *out, cudaStream_t st);
+// a kernel whose bounded wait cannot complete (see csmc_selftest_timeout)
+cudaError_t launch_wait_selftest(int which, unsigned int *ctr, int *error_flag, cudaStream_t st);
 // static shared memory of the selected resident kernel in bytes (-1: query failed)
 template <typename R> int resident_static_smem(const ResidentSel &sel);
 

@@ -77,11 +77,22 @@ __device__ __forceinline__ void bulk_commit_and_wait() {
     asm volatile("cp.async.bulk.commit_group;\n\tcp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-// Bounded wait on an mbarrier phase: gives up after a fixed number of polls
-// and reports it through the context's error flag instead of hanging.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *error_flag) {
-    for (int k = 0; k < (1 << 22); k++)
+// Nanoseconds of the global timer: the time bound of every device wait.
+__device__ __forceinline__ uint64_t gtimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+constexpr uint64_t WAIT_BUDGET_NS = 1000000000ull; // one second
+
+// Bounded wait on an mbarrier phase: gives up after `budget` nanoseconds and
+// reports it through the context's error flag instead of hanging.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *error_flag,
+                                                  uint64_t budget = WAIT_BUDGET_NS) {
+    const uint64_t t0 = gtimer_ns();
+    do {
         if (mbar_try_wait(bar, parity)) return true;
+    } while (gtimer_ns() - t0 < budget);
     if (threadIdx.x == 0) atomicExch(error_flag, 1);
     return false;
 }
@@ -89,10 +100,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 // Barrier across every CTA of a cooperative launch (all CTAs co-resident):
 // a monotonic arrival counter, zero at launch; the k-th barrier of the launch
 // completes when the counter reaches k * n_blocks.  Bounded: thread 0 gives
-// up after a fixed number of polls, or as soon as another CTA has reported an
+// up after `budget` nanoseconds, or as soon as another CTA has reported an
 // error, and sets the error flag.  Returns false (block-uniform) on failure.
 __device__ __forceinline__ bool grid_barrier(unsigned int *ctr, unsigned int n_blocks, unsigned int &epoch,
-                                             int *error_flag, int *s_ok) {
+                                             int *error_flag, int *s_ok, uint64_t budget = WAIT_BUDGET_NS) {
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch++;
@@ -100,7 +111,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *ctr, unsigned int n_b
         atomicAdd(ctr, 1u);
         const unsigned int target = epoch * n_blocks;
         int ok = 0;
-        for (int k = 0; k < (1 << 22); k++) {
+        const uint64_t t0 = gtimer_ns();
+        for (int k = 0; gtimer_ns() - t0 < budget; k++) {
             unsigned int v;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
             if (v >= target) {
@@ -211,8 +223,8 @@ template <int CL> struct Sync {
     // Barrier across the cluster between colour classes: every CTA first
     // waits for its own threads (bar.sync), then thread 0 arrives on every
     // rank's phase mbarrier and waits, suspended in try_wait, for the
-    // arrivals of all ranks; bounded, reporting a timeout through the
-    // error flag.
+    // arrivals of all ranks; bounded (one second), reporting a timeout
+    // through the error flag.
     __device__ __forceinline__ void bar() const {
         __syncthreads();
         if (CL > 1) {
@@ -222,7 +234,8 @@ template <int CL> struct Sync {
                 for (int r = 0; r < CL; r++) mbar_arrive_cluster(map_rank(a, r));
                 const uint32_t ph = *pphase;
                 bool done = false;
-                for (int k = 0; k < (1 << 22) && !done; k++) done = mbar_try_wait_cluster(pbar, ph);
+                const uint64_t t0 = gtimer_ns();
+                while (!done && gtimer_ns() - t0 < WAIT_BUDGET_NS) done = mbar_try_wait_cluster(pbar, ph);
                 if (!done) atomicExch(error_flag, 1);
                 *pphase = ph ^ 1u;
             }

@@ -85,6 +85,35 @@ template <typename R> int resident_static_smem(const ResidentSel &sel) {
     return (int)at.sharedSizeBytes;
 }
 
+// Self-test of the bounded waits: a wait that can never complete must give
+// up, set the error flag and return.  which = 0: an mbarrier phase that
+// expects 16 bytes no copy delivers (one CTA); which = 1: a grid barrier that
+// expects one more CTA than the launch has (two co-resident CTAs).
+__global__ void k_wait_selftest(int which, unsigned int *ctr, int *error_flag, uint64_t budget) {
+    __shared__ uint64_t bar;
+    __shared__ int s_ok;
+    if (which == 0) {
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);
+        mbar_wait_bounded(&bar, 0, error_flag, budget);
+        __syncthreads();
+    } else {
+        unsigned int epoch = 0;
+        grid_barrier(ctr, gridDim.x + 1, epoch, error_flag, &s_ok, budget);
+    }
+}
+
+cudaError_t launch_wait_selftest(int which, unsigned int *ctr, int *error_flag, cudaStream_t st) {
+    uint64_t budget = 20000000ull; // 20 ms
+    void *args[] = {(void *)&which, (void *)&ctr, (void *)&error_flag, (void *)&budget};
+    if (which == 0) return cudaLaunchKernel((const void *)k_wait_selftest, dim3(1), dim3(64), args, 0, st);
+    return cudaLaunchCooperativeKernel((const void *)k_wait_selftest, dim3(2), dim3(64), args, 0, st);
+}
+
 template cudaError_t launch_resident<float>(const ResSys<float> *, const int2 *, int, int *, const ChainState &,
                                             const RunDesc &, int, int, size_t, const ResidentSel &, bool, cudaStream_t);
 template cudaError_t launch_resident<double>(const ResSys<double> *, const int2 *, int, int *, const ChainState &,

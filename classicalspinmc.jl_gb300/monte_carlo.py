@@ -257,6 +257,29 @@ def get_magnetization(x, slot: int = 0) -> float:
     return float(ctx.per_slot("csmc_magnetization")[slot])
 
 
+def structure_factors(x, ks) -> np.ndarray:
+    """compute_equal_time_correlations (spin_correlations.jl:6-43) of every
+    slot at once: ks is dim x N_k (the reference's layout); returns an array
+    [slot, 9, N_k] of Re(S_a(k) conj(S_b(k))) / N, row 3a+b."""
+    ctx, mc = _context_of(x)
+    lat = mc.lattice if mc is not None else x
+    ks = np.asfortranarray(np.atleast_2d(np.asarray(ks, dtype=np.float64)))
+    pos = np.asfortranarray(lat.site_positions, dtype=np.float64)
+    dim, n_k = ks.shape
+    if pos.shape[0] != dim:
+        raise ValueError(f"ks has {dim} rows, the lattice is {pos.shape[0]}-dimensional")
+    R = ctx.replicas[0]
+    out = np.zeros((R, n_k, 9), np.float64)
+    ctx.call("csmc_structure_factor", 0, dim, _lib.ptr(pos, C.c_double), n_k, _lib.ptr(ks, C.c_double),
+             _lib.ptr(out, C.c_double))
+    return np.ascontiguousarray(out.transpose(0, 2, 1))
+
+
+def compute_equal_time_correlations(x, ks, slot: int = 0) -> np.ndarray:
+    """compute_equal_time_correlations (spin_correlations.jl:6-43) of one slot: 9 x N_k."""
+    return structure_factors(x, ks)[slot]
+
+
 def get_local_field(x, point: int, slot: int = 0) -> tuple:
     """get_local_field (hamiltonian.jl:3-67) at 1-based site `point`."""
     ctx, mc = _context_of(x)

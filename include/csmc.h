@@ -265,6 +265,27 @@ int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_therm
 int csmc_set_cluster_size(void *ctx, int32_t ranks);
 int csmc_cluster_size(void *ctx, int32_t *ranks);
 
+/* compute_equal_time_correlations (spin_correlations.jl:6-43) for every slot
+ * of lattice `lattice`: S_a(k) = sum_i exp(-i k.r_i) s_i,a and
+ * Suv(k)[3a+b] = Re(S_a(k) conj(S_b(k))) / N.  positions: the reference's
+ * site_positions, dim x N column-major (the dim coordinates of a site
+ * contiguous, reference site order); ks: dim x n_k column-major; Suv:
+ * [replicas of the lattice][n_k][9], the reference's 9 x N_k array per slot
+ * in slot order.  Computed in the context's precision (sums of the phases
+ * times the spins), the products of the sums in Float64.  csmc_last_run_stats
+ * reports the kernel's device time. */
+int csmc_structure_factor(void *ctx, int32_t lattice, int32_t dim, const double *positions, int64_t n_k,
+                          const double *ks, double *Suv);
+
+/* Self-test of the bounded device waits (no counterpart in the reference).
+ * Runs a kernel whose wait can never complete -- which = 0: an mbarrier phase
+ * waiting for 16 bytes no copy delivers; which = 1: a grid barrier expecting
+ * one more CTA than the launch has -- and returns what a run returns when a
+ * wait gives up: CSMC_ERR_TIMEOUT after the kernel has set the error flag and
+ * returned (a 20 ms budget here, one second in the sweep kernels); the flag is cleared and the context stays
+ * usable.  Any other code is a failure of the bound. */
+int csmc_selftest_timeout(void *ctx, int32_t which);
+
 /* Persistent exchange windows (a tuning knob of this library; no counterpart
  * in the reference).  On (the default): when every replica of the context is
  * resident on the device at once, csmc_run runs up to 128 exchange windows in

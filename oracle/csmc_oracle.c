@@ -562,6 +562,29 @@ double orc_magnetization(const orc_lattice *l, const double *sp) {
     return norm3(mx, my, mz);
 }
 
+/* compute_equal_time_correlations (spin_correlations.jl:6-43).  The
+ * reference forms the row phase = exp.(-im * k' * pos) (:21) and the products
+ * phase * x (:22-24): exp(-i t) = cos t - i sin t with t = k.r_i summed over
+ * the dimensions in order, then Suv rows (:32-40) divided by lat.size (:42). */
+void orc_structure_factor(const double *sp, int64_t N, const double *pos, int dim, const double *ks, int64_t n_k,
+                          double *Suv) {
+    for (int64_t n = 0; n < n_k; n++) {
+        double re[3] = {0.0, 0.0, 0.0}, im[3] = {0.0, 0.0, 0.0};
+        for (int64_t i = 0; i < N; i++) {
+            double t = 0.0;
+            for (int d = 0; d < dim; d++) t = t + ks[n * dim + d] * pos[i * dim + d];
+            const double c = cos(t), s = -sin(t);
+            for (int a = 0; a < 3; a++) {
+                re[a] = re[a] + c * sp[3 * i + a];
+                im[a] = im[a] + s * sp[3 * i + a];
+            }
+        }
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) /* Re((re_a + i im_a)(re_b - i im_b)) */
+                Suv[n * 9 + 3 * a + b] = (re[a] * re[b] + im[a] * im[b]) / (double)N;
+    }
+}
+
 /* ------------------------------------------------------------------ updates */
 
 static const double TWO_PI = 6.283185307179586; /* 2.0 * pi in Float64 */

@@ -86,6 +86,13 @@ double orc_site_energy(const orc_lattice *lat, const double *spins, int64_t i);
 double orc_total_energy(const orc_lattice *lat, const double *spins);
 double orc_magnetization(const orc_lattice *lat, const double *spins);
 
+/* compute_equal_time_correlations (spin_correlations.jl:6-43): for the n_k
+ * wavevectors ks (dim x n_k, column-major) and site positions pos (dim x N),
+ * S_a(k) = sum_i exp(-i k.r_i) s_i,a and Suv[n*9 + 3a + b] =
+ * Re(S_a(k_n) conj(S_b(k_n))) / N (9 x n_k, column-major). */
+void orc_structure_factor(const double *spins, int64_t N, const double *pos, int dim, const double *ks,
+                          int64_t n_k, double *Suv);
+
 /* Proposals (lattice.jl:306-311, metropolis.jl:84-87) from given uniforms. */
 void orc_random_spin_orientation(double S, double u_phi, double u_z, double out[3]);
 void orc_gaussian_move(double S, const double s[3], double sigma, double u_phi, double u_z,

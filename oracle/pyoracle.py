@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
             "orc_site_energy": (C.c_double, [C.c_void_p, f64p, C.c_int64]),
             "orc_total_energy": (C.c_double, [C.c_void_p, f64p]),
             "orc_magnetization": (C.c_double, [C.c_void_p, f64p]),
+            "orc_structure_factor": (None, [f64p, C.c_int64, f64p, C.c_int, f64p, C.c_int64, f64p]),
             "orc_random_spin_orientation": (None, [C.c_double, C.c_double, C.c_double, f64p]),
             "orc_gaussian_move": (None, [C.c_double, f64p, C.c_double, C.c_double, C.c_double, f64p]),
             "orc_energy_diff": (C.c_double, [C.c_void_p, f64p, C.c_int64, f64p]),
@@ -268,6 +269,18 @@ class OracleLattice:
                   for r in range(R)]
         return dict(energy=E[:n], magnetization=M[:n], accepted=acc, exchanged=exc,
                     spins=[f.reshape(3, self.N, order="F") for f in finals])
+
+
+def structure_factor(spins, pos, ks) -> np.ndarray:
+    """compute_equal_time_correlations (spin_correlations.jl:6-43): spins 3 x N,
+    pos dim x N, ks dim x n_k (column-major) -> Suv 9 x n_k."""
+    spins = np.asfortranarray(spins, np.float64)
+    pos = np.asfortranarray(pos, np.float64)
+    ks = np.asfortranarray(ks, np.float64)
+    n_k = ks.shape[1]
+    out = np.zeros((9, n_k), np.float64, order="F")
+    lib().orc_structure_factor(_p(spins), spins.shape[1], _p(pos), pos.shape[0], _p(ks), n_k, _p(out))
+    return out
 
 
 def philox(ctr, key) -> tuple:

@@ -1,0 +1,64 @@
+"""Equal-time spin correlations (compute_equal_time_correlations,
+spin_correlations.jl:6-43) on the GPU against the oracle's restatement, for
+every slot of a parallel-tempering context, in both precisions.
+
+Tolerances: FP64 1e-10 and FP32 2e-5 relative to N, the largest possible
+|S_a(k)|^2 / N (all spins aligned), since the sums run over N sites in a
+different order (device order) than the oracle's."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import rand_spins
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-10, "fp32": 2e-5}
+
+
+def _wavevectors(lat, n, seed):
+    rng = np.random.default_rng(seed)
+    D = lat.site_positions.shape[0]
+    ks = rng.uniform(-np.pi, np.pi, size=(D, n))
+    ks[:, 0] = 0.0  # k = 0: |M|^2 / N
+    return ks
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name,shape,R", [("square", (8, 8), 3), ("honeycomb", (6, 5), 2), ("sc", (6, 6, 6), 17),
+                                          ("pyrochlore", (2, 2, 3), 1)])
+def test_structure_factor_matches_oracle(m, orc, name, shape, R, precision):
+    E = m.examples
+    uc = {"square": E.square_heisenberg, "honeycomb": lambda: E.honeycomb_kitaev(K=-1, J=0.1, G=0.05),
+          "sc": E.sc_heisenberg, "pyrochlore": E.pyrochlore_ckq}[name]()
+    lat = m.Lattice(shape, uc, 1.0)
+    mc = m.MonteCarlo([0.5 + 0.1 * r for r in range(R)] if R > 1 else 0.5, lat, {}, precision=precision, seed=5)
+    spins = [rand_spins(lat.size, 70 + r) for r in range(R)]
+    for r, s in enumerate(spins):
+        mc.set_spins(s, r)
+    ks = _wavevectors(lat, 77, 3)  # n_k not a multiple of the 64-wavevector tile
+    got = m.structure_factors(mc, ks)
+    assert got.shape == (R, 9, 77)
+    for r in range(R):
+        ref = orc.structure_factor(mc.spins(r), lat.site_positions, ks)
+        assert np.abs(got[r] - ref).max() <= TOL[precision] * lat.size, (r, np.abs(got[r] - ref).max())
+    # k = 0 is |sum_i s_i|^2 / N
+    for r in range(R):
+        assert got[r][0, 0] + got[r][4, 0] + got[r][8, 0] == pytest.approx(
+            m.get_magnetization(mc, r) ** 2 / lat.size, rel=1e-4 if precision == "fp32" else 1e-10)
+
+
+def test_structure_factor_follows_the_slots_after_exchanges(m, orc):
+    """The record is by slot: after a PT run with exchanges, slot r's
+    correlations are those of the configuration now in slot r."""
+    lat = m.Lattice((6, 6), m.examples.triangular_afm(h=0.5), 1.0)
+    mc = m.MonteCarlo([0.2, 0.3, 0.5, 0.8], lat, {"overrelaxation_rate": 5}, precision="fp64", seed=2)
+    p = mc.parameters
+    p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 0, 50, 50, 10
+    p.probe_rate, p.swap_rate = 5, 5
+    m.parallel_tempering(mc, verbose=False)
+    assert mc.exchanged.sum() > 0
+    ks = _wavevectors(lat, 9, 4)
+    got = m.structure_factors(mc, ks)
+    for r in range(4):
+        ref = orc.structure_factor(mc.spins(r), lat.site_positions, ks)
+        assert np.abs(got[r] - ref).max() <= 1e-10 * lat.size
