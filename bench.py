@@ -53,6 +53,7 @@ ITER_PER_STEP = 100
 SEED = 20261203
 BYTES_PER_UPDATE_FP32 = 12 * (2 + 6)  # s_b * (2 + z): own spin read+write, 6 neighbours read
 RESIDENT_BLOCK = 0
+RUN_PATH = 0  # CSMC_PATH_AUTO; --path selects another execution path
 
 
 def workload_config(extra=None):
@@ -118,7 +119,8 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def run_params(L, start, n, rec_E=None, rec_M=None, cap=0, path=0):
+def run_params(L, start, n, rec_E=None, rec_M=None, cap=0, path=None):
+    path = RUN_PATH if path is None else path
     rp = L.RunParams()
     rp.sweep_start = start
     rp.n_sweeps = n
@@ -207,6 +209,9 @@ def bench_ours(args, rank, world, dist):
     out = {"value": value, "ms_per_step": 1e3 * t_dev / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
            "gpu_launches": launches, "clocks": clk.summary(), "ctas_per_replica": ranks.value, "autotune": tuned}
     # roofline of the dominant kernel (the resident sweep kernel, one launch per step)
+    kernel = "k_resident<float>"
+    if kern_launches == 0:  # global path: every launch of a step (colour sweeps, energies, exchange)
+        kern_ms, kern_launches, kernel = dev_ms, args.steps, "global colour sweeps (whole step)"
     per_launch_s = kern_ms / 1e3 / max(kern_launches, 1)
     bytes_per_launch = upd * BYTES_PER_UPDATE_FP32 * args.steps / max(kern_launches, 1)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -215,14 +220,14 @@ def bench_ours(args, rank, world, dist):
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("k_resident_fp32_sc_L24_R64")
+        traffic = json.loads(tf.read_text()).get("k_resident_fp32_sc_L24_R64") if kernel.startswith("k_res") else None
     # the level that binds: the replicas stay in shared memory, so the same
     # algorithmic bytes are also set against the nominal shared-memory
     # bandwidth of the SMs in use (128 B per clock per SM)
     sm_mhz = (clk.summary().get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0))
     smem_peak = 152 * 128 * sm_mhz * 1e6 / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                       "traffic": traffic, "kernel": "k_resident<float>",
+                       "traffic": traffic, "kernel": kernel,
                        "kernel_ms_per_launch": per_launch_s * 1e3, "algorithmic_bytes_per_launch": bytes_per_launch,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
                        "note": "replicas resident in shared memory for whole launches: achieved is the algorithmic "
@@ -455,6 +460,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per CTA of the resident kernel (0: library default)")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica (0: autotuned; 1, 2 or 4)")
     ap.add_argument("--no-autotune", action="store_true", help="skip csmc_autotune (library heuristics)")
+    ap.add_argument("--path", default="auto", choices=["auto", "resident", "global"],
+                    help="execution path of csmc_run (auto: the autotuner's choice)")
     ap.add_argument("--no-persistent", action="store_true",
                     help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",
@@ -469,8 +476,9 @@ def main():
     if args.workload != "sc_pt":
         bench_other(args)
         return
-    global RESIDENT_BLOCK
+    global RESIDENT_BLOCK, RUN_PATH
     RESIDENT_BLOCK = args.block
+    RUN_PATH = {"auto": 0, "resident": 1, "global": 2}[args.path]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     threads = os.cpu_count() or 1

@@ -176,6 +176,8 @@ class MonteCarlo:
         for r in range(R):
             self.ctx.set_spins(r, self.lattice.spins)
         self.observables = [Observables() for _ in range(R)]
+        self.corr = bool(corr)  # monte_carlo.jl:81-82
+        self.momentum_vectors = None if ks is None else np.asfortranarray(ks, dtype=np.float64)
         self.accepted = np.zeros(R)
         self.exchanged = np.zeros(R)
 
@@ -372,32 +374,33 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     total = p.t_thermalization + p.t_measurement
     Es, Ms = [], []
     start = 0
+
+    def pieces(a, b):
+        """[a, b) split after every probe iteration when correlations are measured
+        (monte_carlo.jl:371-375 computes them at the probe, after the exchange)."""
+        if not mc.corr or p.probe_rate <= 0:
+            return [(a, b)]
+        out, q = [], a
+        for it in range(a, b):
+            if it >= p.t_thermalization and it % p.probe_rate == 0:
+                out.append((q, it + 1))
+                q = it + 1
+        if q < b:
+            out.append((q, b))
+        return out
+
     while start < total:
         n = min(p.report_interval, total - start)
-        cap = n // max(p.probe_rate, 1) + 2
-        rec_E = np.zeros((cap, R))
-        rec_M = np.zeros((cap, R))
         acc = np.zeros(R)
         exc = np.zeros(R)
-        rp = _lib.RunParams()
-        rp.sweep_start = start
-        rp.n_sweeps = n
-        rp.t_thermalization = p.t_thermalization
-        rp.overrelaxation_rate = p.overrelaxation_rate
-        rp.swap_rate = p.swap_rate if R > 1 else 0
-        rp.probe_rate = p.probe_rate
-        rp.kind = alg.kind
-        rp.path = _PATHS[mc.path]
-        rp.resident_block = resident_block
-        rp.probe_energy = _lib.ptr(rec_E, C.c_double)
-        rp.probe_magnetization = _lib.ptr(rec_M, C.c_double)
-        rp.probe_capacity = cap
-        rp.accepted = _lib.ptr(acc, C.c_double)
-        rp.exchanged = _lib.ptr(exc, C.c_double)
-        mc.ctx.call("csmc_run", C.byref(rp))
-        k = rp.n_probes_out
-        Es.append(rec_E[:k])
-        Ms.append(rec_M[:k])
+        for a, b in pieces(start, start + n):
+            k, E_, M_ = _run_piece(mc, a, b - a, alg, resident_block, acc, exc)
+            Es.append(E_[:k])
+            Ms.append(M_[:k])
+            if mc.corr and b - 1 >= p.t_thermalization and p.probe_rate > 0 and (b - 1) % p.probe_rate == 0:
+                ssf = structure_factors(mc, mc.momentum_vectors)
+                for r in range(R):
+                    mc.observables[r].push_correlations(ssf[r])
         mc.accepted += acc
         mc.exchanged += exc
         start += n
@@ -410,6 +413,33 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
             mc.observables[r].push(e, m)
     mc.sync()
     return {"energy": E, "magnetization": M, "summary": summarize(mc, E, M)}
+
+
+def _run_piece(mc, start, n, alg, resident_block, acc, exc):
+    """csmc_run over iterations [start, start + n) with the PT schedule; the
+    probe records and counters of the piece (counters added to acc, exc)."""
+    p = mc.parameters
+    R = mc.n_replicas
+    cap = n // max(p.probe_rate, 1) + 2
+    rec_E = np.zeros((cap, R))
+    rec_M = np.zeros((cap, R))
+    rp = _lib.RunParams()
+    rp.sweep_start = start
+    rp.n_sweeps = n
+    rp.t_thermalization = p.t_thermalization
+    rp.overrelaxation_rate = p.overrelaxation_rate
+    rp.swap_rate = p.swap_rate if R > 1 else 0
+    rp.probe_rate = p.probe_rate
+    rp.kind = alg.kind
+    rp.path = _PATHS[mc.path]
+    rp.resident_block = resident_block
+    rp.probe_energy = _lib.ptr(rec_E, C.c_double)
+    rp.probe_magnetization = _lib.ptr(rec_M, C.c_double)
+    rp.probe_capacity = cap
+    rp.accepted = _lib.ptr(acc, C.c_double)
+    rp.exchanged = _lib.ptr(exc, C.c_double)
+    mc.ctx.call("csmc_run", C.byref(rp))
+    return rp.n_probes_out, rec_E, rec_M
 
 
 def autotune(mc: MonteCarlo, n_windows: int = 4, alg: _Alg | None = None) -> list[dict]:

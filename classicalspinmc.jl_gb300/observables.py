@@ -20,11 +20,20 @@ class Observables:
     def __init__(self):
         self.energy: list[float] = []
         self.magnetization: list[float] = []
+        self.correlations: list[np.ndarray] = []
 
     def push(self, E: float, M: float) -> None:
         """update_observables! (observables.jl:20-25)."""
         self.energy.append(float(E))
         self.magnetization.append(float(M))
+
+    def push_correlations(self, Suv: np.ndarray) -> None:
+        """update_correlations! (observables.jl:27-30): one 9 x N_k sample."""
+        self.correlations.append(np.array(Suv, dtype=np.float64))
+
+    def mean_correlations(self) -> np.ndarray | None:
+        """The mean of the correlation samples (the LogBinner's mean)."""
+        return np.mean(self.correlations, axis=0) if self.correlations else None
 
 
 def _reliable_bins(x: np.ndarray, min_bins: int = 32) -> np.ndarray:

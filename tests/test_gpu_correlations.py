@@ -25,7 +25,7 @@ def _wavevectors(lat, n, seed):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("name,shape,R", [("square", (8, 8), 3), ("honeycomb", (6, 5), 2), ("sc", (6, 6, 6), 17),
-                                          ("pyrochlore", (2, 2, 3), 1)])
+                                          ("pyrochlore", (2, 2, 3), 1), ("sc", (4, 4, 4), 40)])
 def test_structure_factor_matches_oracle(m, orc, name, shape, R, precision):
     E = m.examples
     uc = {"square": E.square_heisenberg, "honeycomb": lambda: E.honeycomb_kitaev(K=-1, J=0.1, G=0.05),
@@ -62,3 +62,25 @@ def test_structure_factor_follows_the_slots_after_exchanges(m, orc):
     for r in range(4):
         ref = orc.structure_factor(mc.spins(r), lat.site_positions, ks)
         assert np.abs(got[r] - ref).max() <= 1e-10 * lat.size
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_parallel_tempering_measures_correlations_at_every_probe(m, orc, precision):
+    """MonteCarlo(corr=true, ks) (monte_carlo.jl:371-375): one 9 x N_k sample
+    per probe and slot, taken after the exchange; at k = 0 the trace of a
+    sample is |M|^2 / N of the same probe."""
+    lat = m.Lattice((8, 8), m.examples.triangular_afm(h=0.3), 1.0)
+    ks = _wavevectors(lat, 5, 6)
+    mc = m.MonteCarlo([0.2, 0.4, 0.9], lat, {"overrelaxation_rate": 5}, precision=precision, seed=8, corr=True, ks=ks)
+    p = mc.parameters
+    p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 10, 40, 25, 10
+    p.probe_rate, p.swap_rate = 5, 10
+    out = m.parallel_tempering(mc, verbose=False)
+    n_probes = out["magnetization"].shape[0]
+    assert n_probes == 8
+    for r in range(3):
+        samples = np.array(mc.observables[r].correlations)
+        assert samples.shape == (n_probes, 9, 5)
+        trace0 = samples[:, 0, 0] + samples[:, 4, 0] + samples[:, 8, 0]
+        rel = 1e-4 if precision == "fp32" else 1e-10
+        assert np.allclose(trace0, out["magnetization"][:, r] ** 2 / lat.size, rtol=rel, atol=rel)
