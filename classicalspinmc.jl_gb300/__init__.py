@@ -12,7 +12,7 @@ The package directory name contains a dot, so import it through
 from ._lib import CSMCError, lib  # noqa: F401
 from .lattice import Lattice, get_spin, random_spin_orientation, set_spin  # noqa: F401
 from .monte_carlo import (MCParamsBuffer, Metropolis, MetropolisAdaptive, MetropolisFixedCone,  # noqa: F401
-                          MonteCarlo, SimulationParameters, annealing_temperatures, deterministic_updates,
+                          MetropolisConstraint, MetropolisConstraintAdaptive, Constraint, MonteCarlo, SimulationParameters, annealing_temperatures, deterministic_updates,
                           energy_density, get_local_field, get_magnetization, local_fields, overrelaxation,
                           parallel_tempering, replay, simulated_annealing, total_energy, autotune,
                           compute_equal_time_correlations, structure_factors)

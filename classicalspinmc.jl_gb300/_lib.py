@@ -18,6 +18,7 @@ ERRORS = {1: "CSMC_ERR_INVALID", 2: "CSMC_ERR_OOM", 3: "CSMC_ERR_CUDA", 4: "CSMC
           5: "CSMC_ERR_COLOURING", 6: "CSMC_ERR_UNSUPPORTED"}
 FP64, FP32 = 0, 1
 METROPOLIS, METROPOLIS_ADAPTIVE, METROPOLIS_FIXED_CONE = 0, 1, 2
+METROPOLIS_CONSTRAINT, METROPOLIS_CONSTRAINT_ADAPTIVE = 3, 4
 PATH_AUTO, PATH_RESIDENT, PATH_GLOBAL, PATH_PER_REPLICA = 0, 1, 2, 3
 
 i32p = C.POINTER(C.c_int32)
@@ -51,6 +52,12 @@ class LatticeInfo(C.Structure):
         ("width_quartic", C.c_int32), ("n_matrices", C.c_int32), ("n_cubic_tensors", C.c_int32),
         ("n_quartic_tensors", C.c_int32), ("padded_sites", C.c_int64),
     ]
+
+
+class ConstraintDesc(C.Structure):
+    """csmc_constraint: c = g.V + q |V|^2 + p |V| + c0, V = sum_i w_i s_i."""
+    _fields_ = [("site_weights", f64p), ("g", C.c_double * 3), ("q", C.c_double), ("p", C.c_double),
+                ("c0", C.c_double), ("weight", C.c_double)]
 
 
 class RunParams(C.Structure):
@@ -91,6 +98,10 @@ SIGNATURES = {
     "csmc_set_sigma": (C.c_int, [_vp, f64p]),
     "csmc_get_sigma": (C.c_int, [_vp, f64p]),
     "csmc_get_permutation": (C.c_int, [_vp, i32p]),
+    "csmc_set_sigma0": (C.c_int, [_vp, C.c_double]),
+    "csmc_set_constraint": (C.c_int, [_vp, C.c_int32, C.c_void_p]),
+    "csmc_set_lambda": (C.c_int, [_vp, f64p]),
+    "csmc_get_lambda": (C.c_int, [_vp, f64p]),
     "csmc_local_field": (C.c_int, [_vp, C.c_int32, f64p]),
     "csmc_energy_diff": (C.c_int, [_vp, C.c_int32, C.c_int64, i64p, f64p, f64p]),
     "csmc_energy_diff_static": (C.c_int, [_vp, C.c_int32, C.c_int64, i64p, f64p, f64p]),

@@ -4,6 +4,7 @@
 // (monte_carlo.jl:157-190, :288-388).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -86,6 +87,11 @@ struct System {
     DevBuf<int64_t> xbs, xcs, xqs;
     DevBuf<double> xbm, xct, xqt, xfield, xonsite;
     bool exact_ready = false;
+    // constraint of the constrained Metropolis kinds (csmc_set_constraint):
+    // weights by device position (cw) and by reference site (cw_ref), both
+    // empty for unit weights
+    ConsArgs cons{};
+    DevBuf<double> cw, cw_ref;
 };
 
 struct Ctx {
@@ -113,6 +119,8 @@ struct Ctx {
     int cl = 1;         // CTAs per replica of the resident kernel
     int block_pref = 0; // threads per CTA chosen by csmc_autotune (0: automatic)
     bool global_pref = false; // csmc_autotune found the global path faster for CSMC_PATH_AUTO runs
+    DevBuf<double> lambda_slot; // mc.lambda per slot (constrained kinds)
+    double sigma0 = 60.0;       // mc.sigma0 (constrained adaptive kind)
     uint32_t msweep = 0;   // Metropolis sweeps so far (the Philox counter)
     uint64_t nsweeps = 0;  // sweeps of every kind so far (renormalisation cadence)
     int renorm_every = 64;
@@ -522,6 +530,11 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     CK(cudaDeviceGetAttribute(&C->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, C->device));
     CK(cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking));
     C->n_chains = chains;
+    // With a tool injected into the process (CUDA_INJECTION64_PATH: kernel
+    // profilers), multi-window cooperative launches are not issued: such tools
+    // serialise and intercept every launch, and a cooperative cluster launch
+    // under one failed to start.  Exchange windows then run one launch each.
+    if (std::getenv("CUDA_INJECTION64_PATH")) C->persistent_ok = false;
     for (auto &S : C->sys) upload_system(*C, *S);
 
     const int nc = chains;
@@ -537,6 +550,8 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     C->E_chain.upload(zeros);
     C->M_chain.upload(zeros);
     C->last_acc.upload(zeros);
+    C->lambda_slot.upload(zeros);
+    for (auto &S : C->sys) S->cons.lambda_slot = C->lambda_slot.p;
     std::vector<unsigned long long> z64(nc, 0ull);
     C->sweep_acc.upload(z64);
     unsigned int zb = 0;
@@ -697,12 +712,19 @@ struct Launches {
 };
 
 // One sweep of `what` (0 OR, 1 Metropolis, 2 deterministic) over all replicas
-// of every lattice; per_replica issues one launch per replica per class.
+// of every lattice; per_replica issues one launch per replica per class.  The
+// constrained Metropolis kinds are one sequential launch per lattice.
 static void sweep_global(Ctx &C, int what, int kind, double T_override, bool per_replica, Launches &L) {
+    const bool constrained = what == 1 && kind >= CSMC_METROPOLIS_CONSTRAINT;
     for (auto &Sp : C.sys) {
         System &S = *Sp;
         const Plan &P = S.plan;
         with_args(C, S, [&](auto &a) {
+            if (constrained) {
+                launch_metro_constraint(a, C.cs, S.cons, kind, C.msweep, T_override, C.st);
+                L.n++;
+                return;
+            }
             for (int col = 0; col < P.n_colours; col++) {
                 const int64_t st = P.col_start[col], n = P.col_count[col];
                 const int groups = per_replica ? S.R : 1;
@@ -716,7 +738,7 @@ static void sweep_global(Ctx &C, int what, int kind, double T_override, bool per
             }
         });
         if (what == 1) {
-            launch_after_metro(C.cs, S.base, S.R, kind, P.N, C.last_acc.p, C.st);
+            launch_after_metro(C.cs, S.base, S.R, kind, P.N, C.sigma0, C.last_acc.p, C.st);
             L.n++;
         }
     }
@@ -777,7 +799,12 @@ struct Schedule {
     }
 };
 
-static int choose_path(Ctx &C, int requested) {
+static int choose_path(Ctx &C, int requested, int kind) {
+    if (kind >= CSMC_METROPOLIS_CONSTRAINT) {
+        require(requested != CSMC_PATH_RESIDENT, CSMC_ERR_UNSUPPORTED,
+                "the constrained Metropolis kinds run on the global path only (sequential proposals per replica)");
+        return requested == CSMC_PATH_PER_REPLICA ? requested : CSMC_PATH_GLOBAL;
+    }
     if (requested == CSMC_PATH_GLOBAL || requested == CSMC_PATH_PER_REPLICA) return requested;
     bool all = true;
     for (auto &S : C.sys) all = all && S->resident_ok;
@@ -889,7 +916,8 @@ static void run(Ctx &C, csmc_run_params *p) {
     require(p != nullptr, CSMC_ERR_INVALID, "params is NULL");
     require(p->n_sweeps >= 0 && p->sweep_start >= 0, CSMC_ERR_INVALID, "negative sweep range");
     require(p->overrelaxation_rate >= 0, CSMC_ERR_INVALID, "overrelaxation_rate must be >= 0");
-    require(p->kind >= 0 && p->kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(p->kind >= 0 && p->kind <= CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE, CSMC_ERR_INVALID,
+            "unknown Metropolis kind");
     Schedule s;
     s.start = p->sweep_start;
     s.end = p->sweep_start + p->n_sweeps;
@@ -920,7 +948,7 @@ static void run(Ctx &C, csmc_run_params *p) {
     C.acc_slot.zero(C.st);
     C.exch_slot.zero(C.st);
 
-    const int path = choose_path(C, p->path);
+    const int path = choose_path(C, p->path, p->kind);
     C.reset_kernel_time();
     Launches L;
     cudaEvent_t e0 = C.run_e0, e1 = C.run_e1;
@@ -1084,8 +1112,9 @@ static void anneal(Ctx &C, const double *temps, int n_temps, int64_t t_therm, in
                    int path_req, double *accepted) {
     require(n_temps >= 0 && (n_temps == 0 || temps), CSMC_ERR_INVALID, "temperatures missing");
     require(or_rate >= 0, CSMC_ERR_INVALID, "overrelaxation_rate must be >= 0");
-    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
-    const int path = choose_path(C, path_req);
+    require(kind >= 0 && kind <= CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    const int path = choose_path(C, path_req, kind);
+    C.sigma0 = sigma0; // also the reset value of the constrained adaptive kind
     C.reset_kernel_time();
     const int n_slots = C.n_chains;
     Launches L;
@@ -1378,6 +1407,66 @@ int csmc_get_sigma(void *c, double *sigma) {
     API_END
 }
 
+int csmc_set_sigma0(void *c, double sigma0) {
+    API_BEGIN
+    require(std::isfinite(sigma0) && sigma0 >= 0, CSMC_ERR_INVALID, "sigma0 must be finite and >= 0");
+    ctx_of(c).sigma0 = sigma0;
+    API_END
+}
+
+int csmc_set_constraint(void *c, int32_t lattice, const csmc_constraint *k) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(lattice >= 0 && lattice < (int)C.sys.size(), CSMC_ERR_INVALID, "lattice index out of range");
+    System &S = *C.sys[lattice];
+    const Plan &P = S.plan;
+    ConsArgs a{};
+    a.lambda_slot = C.lambda_slot.p;
+    std::vector<double> wd, wr;
+    if (k) {
+        const double vals[7] = {k->g[0], k->g[1], k->g[2], k->q, k->p, k->c0, k->weight};
+        for (double v : vals) require(std::isfinite(v), CSMC_ERR_INVALID, "constraint coefficients must be finite");
+        a.g[0] = k->g[0];
+        a.g[1] = k->g[1];
+        a.g[2] = k->g[2];
+        a.q = k->q;
+        a.p = k->p;
+        a.c0 = k->c0;
+        a.weight = k->weight;
+        if (k->site_weights) {
+            wr.assign(k->site_weights, k->site_weights + P.N);
+            for (double v : wr) require(std::isfinite(v), CSMC_ERR_INVALID, "site weights must be finite");
+            wd.assign((size_t)P.Np, 0.0);
+            for (int64_t d = 0; d < P.Np; d++)
+                if (P.dev2ref[d] >= 0) wd[d] = wr[P.dev2ref[d]];
+        }
+    }
+    CK(cudaStreamSynchronize(C.st)); // no kernel still reads the old weights
+    S.cw.upload(wd);
+    S.cw_ref.upload(wr);
+    a.w = wd.empty() ? nullptr : S.cw.p;
+    S.cons = a;
+    API_END
+}
+
+int csmc_set_lambda(void *c, const double *lambda) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(lambda != nullptr, CSMC_ERR_INVALID, "lambda is NULL");
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaMemcpy(C.lambda_slot.p, lambda, C.n_chains * sizeof(double), cudaMemcpyHostToDevice));
+    API_END
+}
+
+int csmc_get_lambda(void *c, double *lambda) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(lambda != nullptr, CSMC_ERR_INVALID, "lambda is NULL");
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaMemcpy(lambda, C.lambda_slot.p, C.n_chains * sizeof(double), cudaMemcpyDeviceToHost));
+    API_END
+}
+
 int csmc_get_permutation(void *c, int32_t *replica_of_slot) {
     API_BEGIN
     Ctx &C = ctx_of(c);
@@ -1488,7 +1577,7 @@ int csmc_magnetization(void *c, double *M) {
 int csmc_metropolis_sweep(void *c, int32_t kind, double *accepted) {
     API_BEGIN
     Ctx &C = ctx_of(c);
-    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(kind >= 0 && kind <= CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE, CSMC_ERR_INVALID, "unknown Metropolis kind");
     Launches L;
     const uint64_t before = C.nsweeps;
     sweep_global(C, 1, kind, 0.0, false, L);
@@ -1531,7 +1620,8 @@ int csmc_replay(void *c, int32_t slot, int32_t kind, double T, double *sigma, in
     API_BEGIN
     Ctx &C = ctx_of(c);
     require(C.precision == CSMC_FP64, CSMC_ERR_UNSUPPORTED, "replay needs a CSMC_FP64 context");
-    require(kind >= 0 && kind <= 2, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(kind >= 0 && kind <= CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(slot >= 0 && slot < C.n_chains, CSMC_ERR_INVALID, "slot out of range");
     require(n >= 0 && (n == 0 || (sites && u_phi && u_z && u_acc && accepted)), CSMC_ERR_INVALID, "NULL argument");
     require(T > 0, CSMC_ERR_INVALID, "T must be > 0");
     System &S = *C.sys[C.sys_of_slot(slot)];
@@ -1565,9 +1655,20 @@ int csmc_replay(void *c, int32_t slot, int32_t kind, double T, double *sigma, in
     t.ref2dev = S.ref2dev.p;
     t.Np = S.plan.Np;
     t.S = S.plan.desc.S;
+    ExactCons k{};
+    k.w = S.cw_ref.n ? S.cw_ref.p : nullptr;
+    k.g[0] = S.cons.g[0];
+    k.g[1] = S.cons.g[1];
+    k.g[2] = S.cons.g[2];
+    k.q = S.cons.q;
+    k.p = S.cons.p;
+    k.c0 = S.cons.c0;
+    k.weight = S.cons.weight;
+    k.lambda = C.lambda_slot.p + slot;
+    k.sigma0 = C.sigma0;
     if (n > 0)
-        launch_replay(t, S.dspins.p + (size_t)r * 3 * S.plan.Np, kind, T, dsig.p, n, ds.p, dp.p, dz.p, da.p, dacc.p,
-                      C.st);
+        launch_replay(t, k, S.dspins.p + (size_t)r * 3 * S.plan.Np, kind, T, dsig.p, n, ds.p, dp.p, dz.p, da.p,
+                      dacc.p, C.st);
     sync_check(C);
     if (n) CK(cudaMemcpy(accepted, dacc.p, n, cudaMemcpyDeviceToHost));
     if (sigma) CK(cudaMemcpy(sigma, dsig.p, sizeof(double), cudaMemcpyDeviceToHost));
@@ -1658,6 +1759,8 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
     // a run that asks for the global path has nothing to tune; an automatic
     // run also times the global path against the resident configurations
     if (p->path == CSMC_PATH_GLOBAL || p->path == CSMC_PATH_PER_REPLICA) return;
+    // the constrained kinds have a single (sequential) kernel
+    if (p->kind >= CSMC_METROPOLIS_CONSTRAINT) return;
     C.global_pref = false;
     bool resident = true;
     for (auto &S : C.sys) resident = resident && S->resident_ok;

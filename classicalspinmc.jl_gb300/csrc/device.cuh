@@ -10,7 +10,14 @@
 namespace csmc {
 
 // Philox stream purposes (counter word 3); the oracle uses the same values.
-enum : uint32_t { PURPOSE_METRO_A = 1, PURPOSE_METRO_B = 2, PURPOSE_SWAP = 3, PURPOSE_INIT = 4 };
+enum : uint32_t {
+    PURPOSE_METRO_A = 1,
+    PURPOSE_METRO_B = 2,
+    PURPOSE_SWAP = 3,
+    PURPOSE_INIT = 4,
+    PURPOSE_CONS_A = 5, // constrained Metropolis: site and acceptance uniform
+    PURPOSE_CONS_B = 6  // constrained Metropolis: proposal uniforms
+};
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the
 // multiply-xor S-box with Weyl key schedule.

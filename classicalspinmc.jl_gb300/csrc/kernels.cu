@@ -56,6 +56,77 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
     if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&cs.sweep_acc[c], (unsigned long long)acc);
 }
 
+// metropolis_constraint! / metropolis_constraint_adaptive! (metropolis.jl:36-58,
+// 155-179) on every replica of a lattice, one warp per replica: the warp sums
+// the order parameter V of the constraint, then lane 0 makes the sweep's N
+// proposals in sequence -- random site, uniform (kind 3) or cone (kind 4)
+// proposal, dE, the constraint c on V with the proposed spin in place
+// (V updated by the site's weighted change), lambda' = lambda - weight c,
+// acceptance of dE - lambda' c -- since every proposal depends on lambda and V
+// as left by the one before.  Proposal q draws (site, u_acc) from Philox
+// counter (q, msweep, chain, CONS_A) and (u_phi, u_z) from (q, msweep, chain,
+// CONS_B); the site is floor(N x / 2^32) of the first word.
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainState cs, ConsArgs k, int kind,
+                                                        uint32_t msweep, double T_override) {
+    const int r = blockIdx.x;
+    const int c = a.chain_base + r;
+    const Spins<R> p = replica(a, r);
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    for (int64_t d = threadIdx.x; d < a.tb.Np; d += 32) {
+        const V3<R> s = p.get(d);
+        const double w = k.w ? k.w[d] : 1.0;
+        vx += w * (double)s.x;
+        vy += w * (double)s.y;
+        vz += w * (double)s.z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vx += __shfl_xor_sync(0xffffffffu, vx, o);
+        vy += __shfl_xor_sync(0xffffffffu, vy, o);
+        vz += __shfl_xor_sync(0xffffffffu, vz, o);
+    }
+    if (threadIdx.x != 0) return;
+    const int slot = cs.slot_of[c];
+    const double T = T_override > 0 ? T_override : cs.T_slot[slot];
+    const R sigma = (R)cs.sigma_slot[slot];
+    const int pk = kind == CSMC_METROPOLIS_CONSTRAINT ? CSMC_METROPOLIS : CSMC_METROPOLIS_ADAPTIVE;
+    double lambda = k.lambda_slot[slot];
+    unsigned long long acc = 0;
+    const uint64_t n = (uint64_t)a.n_real;
+    for (uint64_t q = 0; q < n; q++) {
+        const U4 A = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
+        const U4 B = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+        const int64_t i = (int64_t)(((uint64_t)A.x * n) >> 32);
+        const int64_t d = a.ref2dev[i];
+        const int b = a.tb.pat[d];
+        V3<R> hb, hc, hq;
+        partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
+        const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
+        const V3<R> s = p.get(d);
+        const V3<R> sn = propose<R>(pk, a.S, sigma, s, (R)u53(B.x, B.y), (R)u53(B.z, B.w));
+        const R dE = delta_e<R>(a.cf, b, s, sn, hext);
+        const double w = k.w ? k.w[d] : 1.0;
+        const double nx = vx + w * ((double)sn.x - (double)s.x);
+        const double ny = vy + w * ((double)sn.y - (double)s.y);
+        const double nz = vz + w * ((double)sn.z - (double)s.z);
+        const double cv = constraint_value(k, nx, ny, nz);
+        const double nl = lambda - k.weight * cv;
+        const double x = (double)dE - nl * cv;
+        const bool accept = x < 0 ? true : u53(A.z, A.w) < exp(-x / T);
+        if (accept) {
+            p.set(d, sn);
+            vx = nx;
+            vy = ny;
+            vz = nz;
+            lambda = nl;
+            acc++;
+        }
+    }
+    k.lambda_slot[slot] = lambda;
+    cs.sweep_acc[c] += acc;
+}
+
 // overrelaxation! body (monte_carlo.jl:128-137) on one colour class.
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
@@ -144,8 +215,10 @@ __global__ void k_reduce_rows(const double *part, int64_t nblk, int width, doubl
 
 // After one Metropolis sweep of replicas [chain_base+lo, +n): move the sweep's
 // accepted count into the slot counters and adapt sigma like
-// metropolis_adaptive! (metropolis.jl:124-126).
-__global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, double n_sites, double *last_acc) {
+// metropolis_adaptive! (metropolis.jl:124-126) or
+// metropolis_constraint_adaptive! (:175-177).
+__global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, double n_sites, double sigma0,
+                              double *last_acc) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int c = chain_first + k;
@@ -161,6 +234,10 @@ __global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, d
         double s = cs.sigma_slot[slot] * f;
         s = s < 0.0 ? 0.0 : (s > 100 ? 100 : s);
         cs.sigma_slot[slot] = s;
+    } else if (kind == CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE) { // metropolis.jl:175-177
+        const double rate = a / n_sites;
+        const double f = 0.5 / (1 - rate);
+        cs.sigma_slot[slot] = rate < 0.5 ? cs.sigma_slot[slot] * f : sigma0;
     }
 }
 
@@ -331,10 +408,17 @@ void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int 
     k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 3, cs.M_chain, a.chain_base, chain_lo);
 }
 
-void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double *last_acc,
-                        cudaStream_t st) {
+void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double sigma0,
+                        double *last_acc, cudaStream_t st) {
     if (n <= 0) return;
-    k_after_metro<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, kind, (double)n_sites, last_acc);
+    k_after_metro<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, kind, (double)n_sites, sigma0, last_acc);
+}
+
+template <typename R>
+void launch_metro_constraint(const SysArgs<R> &a, const ChainState &cs, const ConsArgs &k, int kind, uint32_t msweep,
+                             double T_override, cudaStream_t st) {
+    if (a.n_rep <= 0 || a.n_real <= 0) return;
+    DISPATCH_CQ(a, k_metro_constraint, <<<a.n_rep, 32, 0, st>>>(a, cs, k, kind, msweep, T_override));
 }
 
 void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,
@@ -377,6 +461,8 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
 #define INSTANTIATE(R)                                                                                                 \
     template void launch_metro_colour<R>(const SysArgs<R> &, const ChainState &, int64_t, int64_t, int, int, int,     \
                                          uint32_t, double, cudaStream_t);                                              \
+    template void launch_metro_constraint<R>(const SysArgs<R> &, const ChainState &, const ConsArgs &, int, uint32_t, \
+                                             double, cudaStream_t);                                                    \
     template void launch_or_colour<R>(const SysArgs<R> &, int64_t, int64_t, int, int, cudaStream_t);                  \
     template void launch_det_colour<R>(const SysArgs<R> &, int64_t, int64_t, int, int, cudaStream_t);                 \
     template void launch_energy<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \

@@ -36,6 +36,21 @@ template <typename R> struct SysArgs {
     int cub, qua;
 };
 
+// The closed-form constraint of one lattice (csmc_constraint) for the
+// constrained Metropolis kinds: c = g.V + q |V|^2 + p |V| + c0 with
+// V = sum_d w[d] s_d over device positions (w zero at padding; w == nullptr:
+// weight 1 everywhere, padding spins being zero).
+struct ConsArgs {
+    const double *w;
+    double g[3], q, p, c0, weight;
+    double *lambda_slot; // mc.lambda of every slot
+};
+
+__host__ __device__ __forceinline__ double constraint_value(const ConsArgs &k, double vx, double vy, double vz) {
+    const double vv = vx * vx + vy * vy + vz * vz;
+    return k.g[0] * vx + k.g[1] * vy + k.g[2] * vz + k.q * vv + k.p * sqrt(vv) + k.c0;
+}
+
 // One lattice for the resident kernel (lives in device memory).
 template <typename R> struct ResSys {
     Tab<uint16_t> tb;

@@ -24,8 +24,12 @@ void launch_energy(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int 
 template <typename R>
 void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
                    cudaStream_t st);
-void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double *last_acc,
-                        cudaStream_t st);
+void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double sigma0,
+                        double *last_acc, cudaStream_t st);
+// one constrained Metropolis sweep (kind 3 or 4) of every replica of a lattice
+template <typename R>
+void launch_metro_constraint(const SysArgs<R> &a, const ChainState &cs, const ConsArgs &k, int kind, uint32_t msweep,
+                             double T_override, cudaStream_t st);
 // Exchange of every lattice (lattices[k] = {first slot, replicas}) at
 // iteration `it`, then, if kq >= 0, probe record kq of every slot.
 void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,
@@ -73,9 +77,18 @@ struct ExactTables {
     int64_t Np;
     double S;
 };
+// The constraint of the replayed slot for the constrained kinds: weights in
+// reference site order (nullptr: all 1), the slot's lambda (updated in
+// place) and sigma0 of the adaptive rule.
+struct ExactCons {
+    const double *w;
+    double g[3], q, p, c0, weight;
+    double *lambda;
+    double sigma0;
+};
 // Sequential FP64 replay of n proposals on the FP64 replica at `spins`.
-void launch_replay(const ExactTables &t, double *spins, int kind, double T, double *sigma_dev, int64_t n,
-                   const int64_t *sites, const double *u_phi, const double *u_z, const double *u_acc,
+void launch_replay(const ExactTables &t, const ExactCons &k, double *spins, int kind, double T, double *sigma_dev,
+                   int64_t n, const int64_t *sites, const double *u_phi, const double *u_z, const double *u_acc,
                    uint8_t *accepted, cudaStream_t st);
 
 } // namespace csmc

@@ -84,6 +84,59 @@ def MetropolisFixedCone() -> _Alg:
     return _Alg(_lib.METROPOLIS_FIXED_CONE, "MetropolisFixedCone")
 
 
+def MetropolisConstraint() -> _Alg:
+    """MetropolisConstraint() -> metropolis_constraint! (metropolis.jl:36-58, :193-195).
+
+    The reference's body calls ``e_diff``, which the package does not define;
+    here the proposal is the uniform one of metropolis! (calculate_energy_diff!
+    without a cone, metropolis.jl:94-101)."""
+    return _Alg(_lib.METROPOLIS_CONSTRAINT, "MetropolisConstraint")
+
+
+def MetropolisConstraintAdaptive() -> _Alg:
+    """MetropolisConstraintAdaptive() -> metropolis_constraint_adaptive! (metropolis.jl:155-179, :197-199)."""
+    return _Alg(_lib.METROPOLIS_CONSTRAINT_ADAPTIVE, "MetropolisConstraintAdaptive")
+
+
+class Constraint:
+    """The ``constraint`` function of MonteCarlo (monte_carlo.jl:57) in the
+    closed form the device evaluates: with V = sum_i w_i s_i over the sites
+    (``site_weights`` w in site order, default 1 everywhere),
+
+        c(lattice) = g . V + q |V|^2 + p |V| + c0.
+
+    A linear constraint on the magnetisation along an axis, on its square or
+    on its norm, on a staggered magnetisation (weights +1/-1), and sums of
+    these, have this form.  Calling the object on a lattice or on a 3 x N spin
+    array evaluates c on the host."""
+
+    def __init__(self, site_weights=None, g=(0.0, 0.0, 0.0), q: float = 0.0, p: float = 0.0, c0: float = 0.0):
+        self.site_weights = None if site_weights is None else np.ascontiguousarray(site_weights, np.float64)
+        self.g = tuple(float(x) for x in g)
+        if len(self.g) != 3:
+            raise ValueError("g has 3 components")
+        self.q, self.p, self.c0 = float(q), float(p), float(c0)
+
+    def __call__(self, lattice_or_spins) -> float:
+        s = getattr(lattice_or_spins, "spins", lattice_or_spins)
+        s = np.asarray(s, dtype=np.float64)
+        w = np.ones(s.shape[1]) if self.site_weights is None else self.site_weights
+        V = (s * w).sum(axis=1)
+        vv = float(V @ V)
+        return float(np.dot(self.g, V)) + self.q * vv + self.p * np.sqrt(vv) + self.c0
+
+    def desc(self, n_sites: int, weight: float) -> "_lib.ConstraintDesc":
+        d = _lib.ConstraintDesc()
+        if self.site_weights is not None:
+            if self.site_weights.shape != (n_sites,):
+                raise ValueError(f"site_weights must have one entry per site ({n_sites})")
+            d.site_weights = _lib.ptr(self.site_weights, C.c_double)
+        for a in range(3):
+            d.g[a] = self.g[a]
+        d.q, d.p, d.c0, d.weight = self.q, self.p, self.c0, float(weight)
+        return d
+
+
 _PRECISION = {"fp64": _lib.FP64, "fp32": _lib.FP32}
 _PATHS = {"auto": _lib.PATH_AUTO, "resident": _lib.PATH_RESIDENT, "global": _lib.PATH_GLOBAL,
           "per_replica": _lib.PATH_PER_REPLICA}
@@ -159,8 +212,9 @@ class MonteCarlo:
                  path: str = "auto"):
         if corr and (ks is None or np.asarray(ks).shape[1] == 0):
             raise ValueError("No momentum vectors provided for correlation calculations!")
-        if constraint is not None and weight != 0.0:
-            raise NotImplementedError("constrained Metropolis (metropolis.jl:36-58) is not provided")
+        if constraint is not None and not isinstance(constraint, Constraint):
+            raise TypeError("constraint must be a Constraint: the device evaluates c = g.V + q|V|^2 + p|V| + c0 "
+                            "of V = sum_i w_i s_i, not an arbitrary function")
         if outpath:
             warnings.warn("outpath given: HDF5 output is not written by this package")
         self.temperatures = np.atleast_1d(np.asarray(T, dtype=np.float64)).copy()
@@ -173,6 +227,10 @@ class MonteCarlo:
         self.ctx = Context([self.lattice], [R], precision=precision, seed=seed)
         self.ctx.set_temperatures(self.temperatures)
         self.ctx.call("csmc_set_sigma", _lib.ptr(np.full(R, self.sigma0), C.c_double))
+        self.ctx.call("csmc_set_sigma0", C.c_double(self.sigma0))
+        self.constraint, self.weight = constraint, float(weight)  # monte_carlo.jl:77-78
+        if constraint is not None:
+            self.ctx.call("csmc_set_constraint", 0, C.byref(constraint.desc(self.lattice.size, weight)))
         for r in range(R):
             self.ctx.set_spins(r, self.lattice.spins)
         self.observables = [Observables() for _ in range(R)]
@@ -189,6 +247,18 @@ class MonteCarlo:
     @property
     def n_replicas(self) -> int:
         return len(self.temperatures)
+
+    @property
+    def lambda_(self):
+        """mc.lambda (metropolis.jl:21) per slot: the running Lagrange
+        multiplier of the constrained kinds, 0 at creation."""
+        lm = self.ctx.per_slot("csmc_get_lambda")
+        return float(lm[0]) if len(lm) == 1 else lm
+
+    @lambda_.setter
+    def lambda_(self, value):
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(value, np.float64), (self.n_replicas,)))
+        self.ctx.call("csmc_set_lambda", _lib.ptr(v, C.c_double))
 
     @property
     def sigma(self):
@@ -320,7 +390,8 @@ def simulated_annealing(mc: MonteCarlo, schedule, T0: float = 1.0, alg: _Alg | N
     """
     alg = Metropolis() if alg is None else alg
     if not isinstance(alg, _Alg):
-        raise NotImplementedError("alg must be Metropolis(), MetropolisAdaptive() or MetropolisFixedCone()")
+        raise NotImplementedError("alg must be one of Metropolis(), MetropolisAdaptive(), MetropolisFixedCone(), "
+                                  "MetropolisConstraint(), MetropolisConstraintAdaptive()")
     if len(set(mc.temperatures.tolist())) != 1:
         raise ValueError("simulated_annealing needs one target temperature for all replicas")
     temps = annealing_temperatures(schedule, T0, float(mc.temperatures[0]))
@@ -362,7 +433,8 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     """
     alg = Metropolis() if alg is None else alg
     if not isinstance(alg, _Alg):
-        raise NotImplementedError("alg must be Metropolis(), MetropolisAdaptive() or MetropolisFixedCone()")
+        raise NotImplementedError("alg must be one of Metropolis(), MetropolisAdaptive(), MetropolisFixedCone(), "
+                                  "MetropolisConstraint(), MetropolisConstraintAdaptive()")
     p = mc.parameters
     if p.report_interval == 0:
         raise ZeroDivisionError("integer division error: report_interval is 0 (monte_carlo.jl:383)")

@@ -53,6 +53,10 @@ extern "C" {
 #define CSMC_METROPOLIS 0           /* Metropolis()          -> metropolis!            :65-82   */
 #define CSMC_METROPOLIS_ADAPTIVE 1  /* MetropolisAdaptive()  -> metropolis_adaptive!   :113-133 */
 #define CSMC_METROPOLIS_FIXED_CONE 2 /* MetropolisFixedCone() -> metropolis_fixed_cone! :136-153 */
+/* the constrained kinds (csmc_constraint): N proposals at random sites per
+ * sweep, sequential per replica as in the reference, global path only */
+#define CSMC_METROPOLIS_CONSTRAINT 3          /* MetropolisConstraint()         -> metropolis_constraint!          :36-58  */
+#define CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE 4 /* MetropolisConstraintAdaptive() -> metropolis_constraint_adaptive! :155-179 */
 
 /* execution path of the multi-sweep drivers */
 #define CSMC_PATH_AUTO 0
@@ -193,6 +197,34 @@ int csmc_set_temperatures(void *ctx, const double *T);
 /* mc.sigma per slot (monte_carlo.jl:79, metropolis.jl:84-87). */
 int csmc_set_sigma(void *ctx, const double *sigma);
 int csmc_get_sigma(void *ctx, double *sigma);
+/* mc.sigma0 (monte_carlo.jl:80) of every slot: the cone width that
+ * metropolis_constraint_adaptive! returns to after a sweep accepting at least
+ * half of its proposals (metropolis.jl:177).  Default 60. */
+int csmc_set_sigma0(void *ctx, double sigma0);
+
+/* The `constraint` and `weight` of MonteCarlo (monte_carlo.jl:57,77-78) in a
+ * closed form the device evaluates.  The reference takes any Julia function
+ * of the lattice; here it is a function of the order parameter
+ *     V = sum_i w_i s_i      (w_i = site_weights[i] in reference site order,
+ *                             or 1 for every site when site_weights is NULL):
+ *     c(lattice) = g . V + q |V|^2 + p |V| + c0.
+ * Linear, quadratic and norm constraints on the uniform or on a staggered
+ * magnetisation have this form.  Each constrained proposal evaluates c with
+ * the proposed spin in place, sets lambda' = lambda - weight c and accepts
+ * when dE - lambda' c < 0 or u < exp(-(dE - lambda' c) / T); an accepted
+ * proposal keeps lambda' (metropolis.jl:43-54). */
+typedef struct {
+    const double *site_weights; /* [n_sites] or NULL */
+    double g[3];
+    double q, p, c0;
+    double weight;
+} csmc_constraint;
+/* Constraint of every slot of lattice `lattice` (0-based, creation order);
+ * NULL restores the reference's default x -> 0.0 with weight 0. */
+int csmc_set_constraint(void *ctx, int32_t lattice, const csmc_constraint *constraint);
+/* mc.lambda (metropolis.jl:21) of every slot; 0 at creation. */
+int csmc_set_lambda(void *ctx, const double *lambda);
+int csmc_get_lambda(void *ctx, double *lambda);
 /* For each slot, the physical replica whose spins sit there. */
 int csmc_get_permutation(void *ctx, int32_t *replica_of_slot);
 
@@ -227,7 +259,10 @@ int csmc_magnetization(void *ctx, double *M);
 
 /* alg(mc, T): one Metropolis sweep on every slot at its temperature
  * (metropolis.jl:65-153).  The sweep visits every site once, colour class by
- * colour class.  accepted[n_slots] (or NULL) receives the accepted count. */
+ * colour class; the constrained kinds instead make N proposals at random
+ * sites in sequence, one replica per warp, drawing (site, u_acc) from the
+ * Philox counter (p, sweep, chain, 5) and (u_phi, u_z) from (p, sweep, chain,
+ * 6) for proposal p.  accepted[n_slots] (or NULL) receives the accepted count. */
 int csmc_metropolis_sweep(void *ctx, int32_t kind, double *accepted);
 /* overrelaxation! (monte_carlo.jl:126-139) on every slot. */
 int csmc_overrelax_sweep(void *ctx);
@@ -237,9 +272,12 @@ int csmc_deterministic_sweeps(void *ctx, int64_t n_sweeps);
 
 /* Replay of metropolis!/metropolis_adaptive!/metropolis_fixed_cone!
  * (metropolis.jl:65-153) on one slot, fed with the reference's proposals: n
- * 0-based sites and uniforms.  u_acc[p] is used only where dE >= 0.  FP64,
- * sequential, the reference's evaluation order without FMA contraction.
- * sigma is read (cone kinds) and, for the adaptive kind, updated. */
+ * 0-based sites and uniforms.  u_acc[p] is used only where the exponent
+ * (dE, or dE - lambda' c for the constrained kinds) is >= 0.  FP64,
+ * sequential, the reference's evaluation order without FMA contraction; the
+ * constrained kinds evaluate c over the whole lattice at every proposal, as
+ * the reference calls its constraint function, and update the slot's lambda.
+ * sigma is read (cone kinds) and, for the adaptive kinds, updated. */
 int csmc_replay(void *ctx, int32_t slot, int32_t kind, double T, double *sigma, int64_t n,
                 const int64_t *sites, const double *u_phi, const double *u_z,
                 const double *u_acc, uint8_t *accepted);

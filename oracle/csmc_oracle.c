@@ -675,6 +675,64 @@ int64_t orc_metropolis_replay(const orc_lattice *l, double *sp, double T, int ki
     return acc;
 }
 
+/* ------------------------------------------------- constrained Metropolis */
+
+double orc_constraint_value(const orc_lattice *l, const double *sp, const orc_constraint *k) {
+    double V0 = 0.0, V1 = 0.0, V2 = 0.0;
+    for (int64_t i = 0; i < l->N; i++) {
+        double w = k->w ? k->w[i] : 1.0;
+        V0 = V0 + w * sp[3 * i];
+        V1 = V1 + w * sp[3 * i + 1];
+        V2 = V2 + w * sp[3 * i + 2];
+    }
+    double vv = V0 * V0 + V1 * V1 + V2 * V2;
+    return k->g[0] * V0 + k->g[1] * V1 + k->g[2] * V2 + k->q * vv + k->p * sqrt(vv) + k->c0;
+}
+
+/* One constrained proposal (metropolis.jl:42-55 / 161-174). */
+static int propose_constrained(const orc_lattice *l, double *sp, int64_t i, double T, int cone, double sigma,
+                               double u_phi, double u_z, double u_acc, const orc_constraint *k, double *lambda) {
+    double old[3] = {sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]};
+    double ns[3];
+    if (!cone) orc_random_spin_orientation(l->S, u_phi, u_z, ns);
+    else orc_gaussian_move(l->S, old, sigma, u_phi, u_z, ns);
+    double dE = orc_energy_diff(l, sp, i, ns);
+    double c = orc_constraint_value(l, sp, k);
+    double new_lambda = *lambda - k->weight * c;
+    double x = dE - (new_lambda * c);
+    int accept = x < 0 ? 1 : (u_acc < exp(-(x) / T));
+    if (!accept) {
+        sp[3 * i] = old[0];
+        sp[3 * i + 1] = old[1];
+        sp[3 * i + 2] = old[2];
+    } else {
+        *lambda = new_lambda;
+    }
+    return accept;
+}
+
+/* sigma rule of metropolis_constraint_adaptive! (metropolis.jl:175-177). */
+static double adapt_sigma_constraint(double sigma, double sigma0, double accepted, double n) {
+    double a = accepted / n;
+    double f = 0.5 / (1 - a);
+    return a < 0.5 ? sigma * f : sigma0;
+}
+
+int64_t orc_metropolis_constraint_replay(const orc_lattice *l, double *sp, double T, int cone, double *sigma,
+                                         double sigma0, const orc_constraint *k, double *lambda, int64_t n,
+                                         const int64_t *site, const double *u_phi, const double *u_z,
+                                         const double *u_acc, uint8_t *accepted) {
+    int64_t acc = 0;
+    double sig = sigma ? *sigma : 60.0;
+    for (int64_t p = 0; p < n; p++) {
+        int a = propose_constrained(l, sp, site[p], T, cone, sig, u_phi[p], u_z[p], u_acc[p], k, lambda);
+        if (accepted) accepted[p] = (uint8_t)a;
+        acc += a;
+    }
+    if (cone && sigma) *sigma = adapt_sigma_constraint(sig, sigma0, (double)acc, (double)n);
+    return acc;
+}
+
 /* overrelaxation! body (monte_carlo.jl:127-138). */
 static void overrelax_site(const orc_lattice *l, double *sp, int64_t i) {
     double *s = sp + 3 * i;
@@ -738,7 +796,8 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 }
 
 /* Stream purposes in counter word 3; identical in the GPU kernels. */
-enum { PURPOSE_METRO_A = 1, PURPOSE_METRO_B = 2, PURPOSE_SWAP = 3, PURPOSE_INIT = 4 };
+enum { PURPOSE_METRO_A = 1, PURPOSE_METRO_B = 2, PURPOSE_SWAP = 3, PURPOSE_INIT = 4, PURPOSE_CONS_A = 5,
+       PURPOSE_CONS_B = 6 };
 
 static double u24(uint32_t w) { return (double)(w >> 8) * (1.0 / 16777216.0); }
 static double u53(uint32_t a, uint32_t b) {
@@ -788,6 +847,25 @@ int64_t orc_metropolis_colour_sweep(const orc_lattice *l, double *sp, double T, 
         acc += propose(l, sp, order[d], T, kind, sig, up, uz, colour_u, &ca);
     }
     if (kind == ORC_ADAPTIVE && sigma) *sigma = adapt_sigma(sig, (double)acc, (double)l->N);
+    return acc;
+}
+
+int64_t orc_metropolis_constraint_sweep(const orc_lattice *l, double *sp, double T, int cone, double *sigma,
+                                        double sigma0, const orc_constraint *k, double *lambda, uint64_t seed,
+                                        uint32_t chain, uint32_t sweep) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    double sig = sigma ? *sigma : 60.0;
+    int64_t acc = 0;
+    for (int64_t q = 0; q < l->N; q++) {
+        uint32_t ca[4] = {(uint32_t)q, sweep, chain, PURPOSE_CONS_A}, cb[4] = {(uint32_t)q, sweep, chain, PURPOSE_CONS_B};
+        uint32_t A[4], B[4];
+        orc_philox4x32_10(ca, key, A);
+        orc_philox4x32_10(cb, key, B);
+        int64_t i = (int64_t)(((uint64_t)A[0] * (uint64_t)l->N) >> 32);
+        acc += propose_constrained(l, sp, i, T, cone, sig, u53(B[0], B[1]), u53(B[2], B[3]), u53(A[2], A[3]), k,
+                                   lambda);
+    }
+    if (cone && sigma) *sigma = adapt_sigma_constraint(sig, sigma0, (double)acc, (double)l->N);
     return acc;
 }
 

@@ -113,6 +113,35 @@ int64_t orc_metropolis_replay(const orc_lattice *lat, double *spins, double T, i
                               const double *u_phi, const double *u_z, const double *u_acc,
                               uint8_t *accepted);
 
+/* Constrained Metropolis (metropolis.jl:36-58, 155-179) with the constraint
+ * function in the closed form c = g.V + q |V|^2 + p |V| + c0 of
+ * V = sum_i w_i s_i (w NULL: all 1), evaluated over the whole lattice at every
+ * proposal, as the reference calls mc.constraint(mc.lattice). */
+typedef struct {
+    const double *w;
+    double g[3], q, p, c0;
+    double weight;
+} orc_constraint;
+double orc_constraint_value(const orc_lattice *lat, const double *spins, const orc_constraint *k);
+/* Replay of n proposals: cone = 0 uniform proposals (metropolis_constraint!,
+ * whose e_diff the reference leaves undefined, read as calculate_energy_diff!
+ * with a uniform proposal), cone = 1 cone proposals with *sigma and the
+ * adaptive rule of metropolis_constraint_adaptive! at the end (sigma0 when at
+ * least half accepted).  *lambda is mc.lambda, updated on every acceptance.
+ * u_acc[p] is consumed only when dE - lambda' c >= 0. */
+int64_t orc_metropolis_constraint_replay(const orc_lattice *lat, double *spins, double T, int cone,
+                                         double *sigma, double sigma0, const orc_constraint *k,
+                                         double *lambda, int64_t n, const int64_t *site,
+                                         const double *u_phi, const double *u_z, const double *u_acc,
+                                         uint8_t *accepted);
+/* One constrained sweep of N proposals with the GPU kernel's Philox draws:
+ * proposal q takes counter (q, sweep, chain, 5) for the site floor(N w0 / 2^32)
+ * and u_acc = u53(w2, w3), and (q, sweep, chain, 6) for u_phi = u53(w0, w1),
+ * u_z = u53(w2, w3). */
+int64_t orc_metropolis_constraint_sweep(const orc_lattice *lat, double *spins, double T, int cone,
+                                        double *sigma, double sigma0, const orc_constraint *k,
+                                        double *lambda, uint64_t seed, uint32_t chain, uint32_t sweep);
+
 /* Single-site updates applied in a caller-given order (monte_carlo.jl:126-139
  * and :201-213).  order[] holds 0-based site indices; negative entries are
  * skipped (padding in a device order). */

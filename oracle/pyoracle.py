@@ -40,6 +40,25 @@ class PTParams(C.Structure):
                 ("sigma0", C.c_double), ("n_threads", C.c_int32), ("seed", C.c_uint64)]
 
 
+class Constraint(C.Structure):
+    """orc_constraint: c = g.V + q |V|^2 + p |V| + c0 with V = sum_i w_i s_i."""
+    _fields_ = [("w", f64p), ("g", C.c_double * 3), ("q", C.c_double), ("p", C.c_double), ("c0", C.c_double),
+                ("weight", C.c_double)]
+
+
+def constraint(weights=None, g=(0.0, 0.0, 0.0), q=0.0, p=0.0, c0=0.0, weight=0.0):
+    """An orc_constraint (the weights array is kept alive on the structure)."""
+    k = Constraint()
+    if weights is not None:
+        w = np.ascontiguousarray(weights, np.float64)
+        k._keep = w
+        k.w = w.ctypes.data_as(f64p)
+    for a in range(3):
+        k.g[a] = float(g[a])
+    k.q, k.p, k.c0, k.weight = float(q), float(p), float(c0), float(weight)
+    return k
+
+
 class Rng(C.Structure):
     _fields_ = [("s", C.c_uint64 * 4)]
 
@@ -76,6 +95,13 @@ def lib() -> C.CDLL:
             "orc_energy_diff": (C.c_double, [C.c_void_p, f64p, C.c_int64, f64p]),
             "orc_metropolis_replay": (C.c_int64, [C.c_void_p, f64p, C.c_double, C.c_int, f64p, C.c_int64, i64p,
                                                   f64p, f64p, f64p, u8p]),
+            "orc_constraint_value": (C.c_double, [C.c_void_p, f64p, C.POINTER(Constraint)]),
+            "orc_metropolis_constraint_replay": (C.c_int64, [C.c_void_p, f64p, C.c_double, C.c_int, f64p, C.c_double,
+                                                             C.POINTER(Constraint), f64p, C.c_int64, i64p, f64p,
+                                                             f64p, f64p, u8p]),
+            "orc_metropolis_constraint_sweep": (C.c_int64, [C.c_void_p, f64p, C.c_double, C.c_int, f64p, C.c_double,
+                                                            C.POINTER(Constraint), f64p, C.c_uint64, C.c_uint32,
+                                                            C.c_uint32]),
             "orc_overrelax_order": (None, [C.c_void_p, f64p, i64p, C.c_int64]),
             "orc_deterministic_order": (None, [C.c_void_p, f64p, i64p, C.c_int64]),
             "orc_overrelax_sweep": (None, [C.c_void_p, f64p]),
@@ -211,6 +237,30 @@ class OracleLattice:
         lib().orc_metropolis_replay(self.h, _p(spins), T, kind, C.byref(sg), n, _p(s, C.c_int64), _p(a[0]),
                                     _p(a[1]), _p(a[2]), _p(acc, C.c_uint8))
         return acc, sg.value
+
+    def constraint_value(self, spins, k) -> float:
+        return lib().orc_constraint_value(self.h, _p(spins), C.byref(k))
+
+    def constraint_replay(self, spins, T, cone, sigma, sigma0, k, lam, sites, u_phi, u_z, u_acc):
+        """metropolis_constraint(_adaptive)! fed with the given proposals;
+        returns (accepted flags, sigma, lambda)."""
+        n = len(sites)
+        s = np.ascontiguousarray(sites, np.int64)
+        a = [np.ascontiguousarray(x, np.float64) for x in (u_phi, u_z, u_acc)]
+        acc = np.zeros(n, np.uint8)
+        sg, lm = C.c_double(sigma), C.c_double(lam)
+        lib().orc_metropolis_constraint_replay(self.h, _p(spins), T, int(cone), C.byref(sg), sigma0, C.byref(k),
+                                               C.byref(lm), n, _p(s, C.c_int64), _p(a[0]), _p(a[1]), _p(a[2]),
+                                               _p(acc, C.c_uint8))
+        return acc, sg.value, lm.value
+
+    def constraint_sweep(self, spins, T, cone, sigma, sigma0, k, lam, seed, chain, sweep):
+        """One constrained sweep with the GPU kernel's Philox draws;
+        returns (accepted count, sigma, lambda)."""
+        sg, lm = C.c_double(sigma), C.c_double(lam)
+        acc = lib().orc_metropolis_constraint_sweep(self.h, _p(spins), T, int(cone), C.byref(sg), sigma0,
+                                                    C.byref(k), C.byref(lm), C.c_uint64(seed), chain, sweep)
+        return acc, sg.value, lm.value
 
     def overrelax_order(self, spins, order):
         o = np.ascontiguousarray(order, np.int64)

@@ -104,3 +104,58 @@ def test_replay_matches_direct_energy_difference(m, orc):
         if a:
             t[:, sites[p]] = new
     assert np.array_equal(s, t)
+
+
+def test_constraint_replay_matches_the_reference_loop(m, orc):
+    """The oracle's metropolis_constraint_adaptive! (metropolis.jl:155-179)
+    against the reference's loop written out here: cone proposal, dE,
+    c = constraint(lattice) with the new spin in place, new_lambda =
+    lambda - weight c, accept dE - new_lambda c < 0 or u < exp(-(...)/T),
+    lambda kept on acceptance, sigma rule at the end.  Cubic and quartic
+    terms included (pyrochlore)."""
+    uc = m.examples.pyrochlore_ckq()
+    ol = orc.OracleLattice(uc, (2, 1, 2), 1.0)
+    N = ol.N
+    w = np.linspace(-1.0, 1.0, N)
+    g, q, pn, c0, weight = (0.2, 0.5, -0.3), 0.02, 0.1, -0.7, 0.4
+    k = orc.constraint(w, g=g, q=q, p=pn, c0=c0, weight=weight)
+
+    def c_of(t):
+        V = [0.0, 0.0, 0.0]
+        for i in range(N):
+            for a in range(3):
+                V[a] = V[a] + w[i] * t[a, i]
+        vv = V[0] * V[0] + V[1] * V[1] + V[2] * V[2]
+        return g[0] * V[0] + g[1] * V[1] + g[2] * V[2] + q * vv + pn * math.sqrt(vv) + c0
+
+    s0 = ol.random_spins(seed=3)
+    rng = np.random.default_rng(4)
+    n, T, sigma, sigma0, lam0 = 150, 0.5, 0.6, 9.0, 0.1
+    sites = rng.integers(0, N, n)
+    up, uz, ua = rng.random(n), rng.random(n), rng.random(n)
+    s = s0.copy(order="F")
+    acc, sig, lam = ol.constraint_replay(s, T, 1, sigma, sigma0, k, lam0, sites, up, uz, ua)
+    t, lt, na = s0.copy(order="F"), lam0, 0
+    for p in range(n):
+        i = sites[p]
+        old = t[:, i].copy()
+        phi, z = 2 * math.pi * up[p], 2 * uz[p] - 1
+        r = math.sqrt(1 - z * z)
+        u = np.array([r * math.cos(phi), r * math.sin(phi), z])
+        v = old + sigma * u
+        new = v / math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+        dE = ol.energy_diff(t, i, new)
+        t[:, i] = new
+        c = c_of(t)
+        nl = lt - weight * c
+        x = dE - nl * c
+        a = x < 0 or ua[p] < math.exp(-x / T)
+        assert bool(acc[p]) == a, p
+        if a:
+            lt, na = nl, na + 1
+        else:
+            t[:, i] = old
+    assert np.abs(s - t).max() <= 1e-14
+    assert lam == pytest.approx(lt, rel=1e-12, abs=1e-14)
+    rate = na / n
+    assert sig == pytest.approx(sigma * 0.5 / (1 - rate) if rate < 0.5 else sigma0, rel=1e-15)
