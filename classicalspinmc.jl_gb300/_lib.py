@@ -50,7 +50,8 @@ class LatticeInfo(C.Structure):
         ("n_sites", C.c_int64), ("n_colours", C.c_int32), ("n_bilinear", C.c_int32), ("n_cubic", C.c_int32),
         ("n_quartic", C.c_int32), ("width_bilinear", C.c_int32), ("width_cubic", C.c_int32),
         ("width_quartic", C.c_int32), ("n_matrices", C.c_int32), ("n_cubic_tensors", C.c_int32),
-        ("n_quartic_tensors", C.c_int32), ("padded_sites", C.c_int64),
+        ("n_quartic_tensors", C.c_int32), ("padded_sites", C.c_int64), ("n_isotropic_cubic", C.c_int32),
+        ("n_isotropic_quartic", C.c_int32),
     ]
 
 

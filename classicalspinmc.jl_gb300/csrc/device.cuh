@@ -72,6 +72,8 @@ template <typename R> struct Coef {
     // O+P (dE), O+P/2 (energy share), and the scalar of each bilinear slot
     // when every coupling is a multiple of the identity
     const R *A, *Q, *E2, *Js;
+    // per tensor id: isotropic cubic {flag, kappa}, quartic {flag, q1, q2, q3}
+    const R *ciso, *qiso;
 };
 
 template <typename R> struct V3 {
@@ -173,9 +175,17 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     if (CUB) {
         for (int t = 0; t < tb.W3; t++) {
             const int64_t j = tb.p3[(2 * t) * Np + d], k = tb.p3[(2 * t + 1) * Np + d];
-            const R *C = cf.cubs + 27 * cf.c3[b * tb.W3 + t];
+            const int id = cf.c3[b * tb.W3 + t];
             const V3<R> sj = sv.get(j), sk = sv.get(k);
             using F = Fp<R>;
+            if (cf.ciso[2 * id] != R(0)) { // kappa eps_abc: kappa (s_j x s_k)
+                const R kap = cf.ciso[2 * id + 1];
+                const V3<R> x = {F::fma(sj.y, sk.z, -F::mul(sj.z, sk.y)), F::fma(sj.z, sk.x, -F::mul(sj.x, sk.z)),
+                                 F::fma(sj.x, sk.y, -F::mul(sj.y, sk.x))};
+                hc = add_scaled(hc, kap, x);
+                continue;
+            }
+            const R *C = cf.cubs + 27 * id;
             const R a0 = sj.x, a1 = sj.y, a2 = sj.z, b0 = sk.x, b1 = sk.y, b2 = sk.z;
             const R o[9] = {F::mul(a0, b0), F::mul(a0, b1), F::mul(a0, b2), F::mul(a1, b0), F::mul(a1, b1),
                             F::mul(a1, b2), F::mul(a2, b0), F::mul(a2, b1), F::mul(a2, b2)};
@@ -192,8 +202,16 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     if (QUA) {
         for (int t = 0; t < tb.W4; t++) {
             const int64_t j = tb.p4[(3 * t) * Np + d], k = tb.p4[(3 * t + 1) * Np + d], l = tb.p4[(3 * t + 2) * Np + d];
-            const R *Q = cf.quas + 81 * cf.c4[b * tb.W4 + t];
+            const int id = cf.c4[b * tb.W4 + t];
             const V3<R> sj = sv.get(j), sk = sv.get(k), sl = sv.get(l);
+            if (cf.qiso[4 * id] != R(0)) { // q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k)
+                using F = Fp<R>;
+                const R w1 = F::mul(cf.qiso[4 * id + 1], dot(sk, sl)), w2 = F::mul(cf.qiso[4 * id + 2], dot(sj, sl)),
+                        w3 = F::mul(cf.qiso[4 * id + 3], dot(sj, sk));
+                hq = add_scaled(add_scaled(add_scaled(hq, w1, sj), w2, sk), w3, sl);
+                continue;
+            }
+            const R *Q = cf.quas + 81 * id;
             const R a[3] = {sj.x, sj.y, sj.z}, bb[3] = {sk.x, sk.y, sk.z}, c[3] = {sl.x, sl.y, sl.z};
             using F = Fp<R>;
             R sx = 0, sy = 0, sz = 0;

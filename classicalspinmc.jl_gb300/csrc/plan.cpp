@@ -302,6 +302,60 @@ static void assign_per_basis(Plan &P) {
     }
 }
 
+// The isotropic forms of the deduplicated cubic and quartic tensors (see
+// Plan::cub_iso): the only rotation-invariant rank-3 tensor is eps_abc, the
+// rank-4 ones are the three pairings of delta products.  A tensor is tagged
+// only if it equals the form entry by entry; the kernels then evaluate
+// kappa (s_j x s_k) and q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k)
+// instead of the dense contraction.
+static void classify_isotropic(Plan &P) {
+    auto eps = [](int a, int b, int c) {
+        if (a == b || b == c || a == c) return 0;
+        return ((a + 1) % 3 == b) ? 1 : -1; // (0,1,2) and its cyclic shifts: +1
+    };
+    const size_t nc = P.cubs.size() / 27, nq = P.quas.size() / 81;
+    P.cub_iso.assign(2 * nc, 0.0);
+    for (size_t t = 0; t < nc; t++) {
+        const double *C = &P.cubs[27 * t];
+        const double k = C[(0 * 3 + 1) * 3 + 2];
+        bool ok = true;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                for (int c = 0; c < 3; c++) {
+                    const int e = eps(a, b, c);
+                    const double want = e == 0 ? 0.0 : (e > 0 ? k : -k);
+                    if (C[(a * 3 + b) * 3 + c] != want) ok = false;
+                }
+        if (ok) {
+            P.cub_iso[2 * t] = 1.0;
+            P.cub_iso[2 * t + 1] = k;
+        }
+    }
+    P.qua_iso.assign(4 * nq, 0.0);
+    for (size_t t = 0; t < nq; t++) {
+        const double *Q = &P.quas[81 * t];
+        auto at = [&](int a, int b, int c, int d) { return Q[((a * 3 + b) * 3 + c) * 3 + d]; };
+        const double q1 = at(0, 0, 1, 1), q2 = at(0, 1, 0, 1), q3 = at(0, 1, 1, 0);
+        bool ok = true;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                for (int c = 0; c < 3; c++)
+                    for (int d = 0; d < 3; d++) {
+                        double want = 0.0;
+                        if (a == b && c == d) want += q1;
+                        if (a == c && b == d) want += q2;
+                        if (a == d && b == c) want += q3;
+                        if (at(a, b, c, d) != want) ok = false;
+                    }
+        if (ok) {
+            P.qua_iso[4 * t] = 1.0;
+            P.qua_iso[4 * t + 1] = q1;
+            P.qua_iso[4 * t + 2] = q2;
+            P.qua_iso[4 * t + 3] = q3;
+        }
+    }
+}
+
 static int dedup(std::vector<double> &table, int width, const std::vector<double> &c) {
     int n = (int)(table.size() / width);
     for (int k = 0; k < n; k++)
@@ -599,6 +653,7 @@ Plan make_plan(const csmc_lattice_desc *dd) {
         P.W4 = std::max(P.W4, (int)P.s4[b].size());
     }
 
+    classify_isotropic(P);
     colour_plan(P);
 
     // colour-major device order, each class padded to a multiple of 32 sites,
@@ -761,6 +816,10 @@ void fill_info(const Plan &p, csmc_lattice_info *info) {
     info->n_matrices = (int32_t)(p.mats.size() / 9);
     info->n_cubic_tensors = (int32_t)(p.cubs.size() / 27);
     info->n_quartic_tensors = (int32_t)(p.quas.size() / 81);
+    info->n_isotropic_cubic = 0;
+    info->n_isotropic_quartic = 0;
+    for (size_t t = 0; t < p.cub_iso.size(); t += 2) info->n_isotropic_cubic += p.cub_iso[t] != 0.0;
+    for (size_t t = 0; t < p.qua_iso.size(); t += 4) info->n_isotropic_quartic += p.qua_iso[t] != 0.0;
     info->padded_sites = p.Np;
 }
 

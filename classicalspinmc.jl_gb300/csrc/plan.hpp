@@ -60,6 +60,11 @@ struct Plan {
     int W2 = 0, W3 = 0, W4 = 0; // non-self slot widths of the device tables
     // deduplicated coefficients; id 0 of each table is all zeros
     std::vector<double> mats, cubs, quas;
+    // isotropic forms of the cubic and quartic tensors, per tensor id:
+    // cub_iso {1, kappa} when C[a,b,c] = kappa eps_abc, quartic
+    // qua_iso {1, q1, q2, q3} when R[a,b,c,d] = q1 d_ab d_cd + q2 d_ac d_bd +
+    // q3 d_ad d_bc (exactly); {0, ...} otherwise
+    std::vector<double> cub_iso, qua_iso;
     // colouring and device order
     int n_colours = 0;
     std::vector<int32_t> colour_of;  // reference order

@@ -111,6 +111,8 @@ typedef struct {
     int32_t n_cubic_tensors;
     int32_t n_quartic_tensors;
     int64_t padded_sites;   /* device length of one replica (colour classes padded) */
+    int32_t n_isotropic_cubic;   /* distinct cubic tensors of the form kappa eps_abc */
+    int32_t n_isotropic_quartic; /* distinct quartic tensors q1 d_ab d_cd + q2 d_ac d_bd + q3 d_ad d_bc */
 } csmc_lattice_info;
 
 /* Parameters of a multi-sweep run: the loop of parallel_tempering!

@@ -33,7 +33,7 @@ def test_struct_sizes_match_header(m):
     from importlib import import_module
     L = import_module(m.__name__ + "._lib")
     # 64-bit layouts of csmc_lattice_info / csmc_run_params
-    assert C.sizeof(L.LatticeInfo) == 8 + 10 * 4 + 8
+    assert C.sizeof(L.LatticeInfo) == 8 + 10 * 4 + 8 + 2 * 4
     assert C.sizeof(L.RunParams) == 3 * 8 + 6 * 4 + 2 * 8 + 8 + 2 * 8 + 8
 
 

@@ -32,6 +32,16 @@ def model(m, name):
         return E.triangular_afm(h=0.7), (6, 6), "open"
     if name == "pyrochlore":
         return E.pyrochlore_ckq(), (2, 2, 2), "periodic"
+    if name == "pyrochlore_dense":  # tensors without an isotropic form: the dense contractions
+        uc = E.pyrochlore_ckq(cubic=False, quartic=False)
+        rng = np.random.default_rng(3)
+        C, Q = 0.02 * rng.normal(size=(3, 3, 3)), 0.05 * rng.normal(size=(3, 3, 3, 3))
+        for face in [(1, 2, 3), (2, 3, 4)]:
+            m.addCubic(uc, *face, C, (0, 0, 0), (0, 0, 0))
+        m.addQuartic(uc, 1, 2, 3, 4, Q, (0, 0, 0), (0, 0, 0), (0, 0, 0))
+        m.addQuartic(uc, 1, 3, 2, 4, 0.05 * np.einsum("ab,cd->abcd", np.eye(3), np.eye(3)), (0, 0, 0), (0, 0, 0),
+                     (0, 0, 0))  # isotropic beside dense in one lattice
+        return uc, (2, 2, 2), "periodic"
     if name == "asym_open":
         uc = m.Honeycomb()
         a = np.arange(9.0).reshape(3, 3) / 9 - 0.4
@@ -48,7 +58,7 @@ def model(m, name):
     raise KeyError(name)
 
 
-MODELS = ["square", "honeycomb", "sc", "triangular_open", "pyrochlore", "asym_open", "selfloop"]
+MODELS = ["square", "honeycomb", "sc", "triangular_open", "pyrochlore", "pyrochlore_dense", "asym_open", "selfloop"]
 
 
 def setup(m, orc, name, precision, R=1, seed=20261203, T=1.0):
@@ -156,7 +166,7 @@ def test_overrelax_and_deterministic_in_colour_order(m, orc, name, precision):
 
 
 @pytest.mark.parametrize("kind", ["Metropolis", "MetropolisAdaptive", "MetropolisFixedCone"])
-@pytest.mark.parametrize("name", ["honeycomb", "sc", "pyrochlore", "asym_open"])
+@pytest.mark.parametrize("name", ["honeycomb", "sc", "pyrochlore", "pyrochlore_dense", "asym_open"])
 def test_metropolis_colour_sweep_fp64(m, orc, name, kind):
     """One FP64 colour sweep == the oracle fed the same Philox stream (53-bit uniforms)."""
     seed = 99
@@ -230,7 +240,8 @@ def _run_once(m, mc, start, n, or_rate, path, block=0):
     return acc
 
 
-SINGLE_SWEEP_CASES = [(n, p) for n in ["square", "honeycomb", "sc", "triangular_open", "pyrochlore", "asym_open"]
+SINGLE_SWEEP_CASES = [(n, p) for n in ["square", "honeycomb", "sc", "triangular_open", "pyrochlore", "pyrochlore_dense",
+                                        "asym_open"]
                       for p in ["resident", "resident1024", "global"]] + [("sc24", "global")]
 
 

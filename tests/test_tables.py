@@ -90,6 +90,23 @@ def test_deduplicated_couplings(m):
     assert info.width_bilinear == 6 and info.width_cubic == 6 and info.width_quartic == 6
 
 
+def test_isotropic_tensor_forms(m):
+    """kappa eps_abc and the delta pairings are recognised after the role
+    permutations (lattice.jl:241-291); other tensors keep the dense form."""
+    info = m.Lattice((2, 2, 2), m.examples.pyrochlore_ckq(), 1.0).info
+    assert info.n_isotropic_cubic == info.n_cubic_tensors  # zero tensor, +kappa eps, -kappa eps
+    assert info.n_isotropic_quartic == info.n_quartic_tensors
+    assert info.n_cubic_tensors == 3
+    uc = m.examples.pyrochlore_ckq(cubic=False, quartic=False)
+    rng = np.random.default_rng(1)
+    m.addCubic(uc, 1, 2, 3, rng.normal(size=(3, 3, 3)), (0, 0, 0), (0, 0, 0))
+    iso = 0.3 * np.einsum("ab,cd->abcd", np.eye(3), np.eye(3)) - 0.1 * np.einsum("ac,bd->abcd", np.eye(3), np.eye(3))
+    m.addQuartic(uc, 1, 2, 3, 4, iso, (0, 0, 0), (0, 0, 0), (0, 0, 0))
+    info = m.Lattice((2, 2, 2), uc, 1.0).info
+    assert info.n_isotropic_cubic == 1  # only the zero tensor
+    assert info.n_isotropic_quartic == info.n_quartic_tensors
+
+
 def test_field_assignment_rule(m, orc):
     """lattice.jl:128-139 assigns the i-th field entry to column f_indices[i]."""
     uc = m.Honeycomb()
