@@ -64,8 +64,8 @@ struct System {
     DevBuf<uint8_t> pat;
     DevBuf<int32_t> dev2ref, c2, c3, c4;
     DevBuf<int64_t> ref2dev;
-    DevBuf<float> fmats, fcubs, fquas, fO, fP, fh, fspins, fA, fQ, fE2, fJs, fciso, fqiso;
-    DevBuf<double> dmats, dcubs, dquas, dO, dP, dh, dspins, dA, dQ, dE2, dJs, dciso, dqiso;
+    DevBuf<float> fmats, fcubs, fquas, fO, fP, fh, fspins, fA, fQ, fE2, fJs, fmiso, fciso, fqiso;
+    DevBuf<double> dmats, dcubs, dquas, dO, dP, dh, dspins, dA, dQ, dE2, dJs, dmiso, dciso, dqiso;
     SysArgs<float> fa{};
     SysArgs<double> da{};
     bool resident_ok = false;
@@ -308,6 +308,7 @@ static void upload_system(Ctx &C, System &S) {
         S.fmats.upload(to_f(P.mats));
         S.fcubs.upload(to_f(P.cubs));
         S.fquas.upload(to_f(P.quas));
+        S.fmiso.upload(to_f(P.mat_iso));
         S.fciso.upload(to_f(P.cub_iso));
         S.fqiso.upload(to_f(P.qua_iso));
         S.fO.upload(to_f(O));
@@ -316,6 +317,7 @@ static void upload_system(Ctx &C, System &S) {
         S.fspins.alloc(nsp);
         CK(cudaMemset(S.fspins.p, 0, nsp * sizeof(float)));
         fill_args(S.fa, S.fspins.p, S.fmats.p, S.fcubs.p, S.fquas.p, S.fO.p, S.fP.p, S.fh.p);
+        S.fa.cf.miso = S.fmiso.p;
         S.fa.cf.ciso = S.fciso.p;
         S.fa.cf.qiso = S.fqiso.p;
         S.fA.upload(to_f(A));
@@ -332,6 +334,7 @@ static void upload_system(Ctx &C, System &S) {
         S.dmats.upload(P.mats);
         S.dcubs.upload(P.cubs);
         S.dquas.upload(P.quas);
+        S.dmiso.upload(P.mat_iso);
         S.dciso.upload(P.cub_iso);
         S.dqiso.upload(P.qua_iso);
         S.dO.upload(O);
@@ -340,6 +343,7 @@ static void upload_system(Ctx &C, System &S) {
         S.dspins.alloc(nsp);
         CK(cudaMemset(S.dspins.p, 0, nsp * sizeof(double)));
         fill_args(S.da, S.dspins.p, S.dmats.p, S.dcubs.p, S.dquas.p, S.dO.p, S.dP.p, S.dh.p);
+        S.da.cf.miso = S.dmiso.p;
         S.da.cf.ciso = S.dciso.p;
         S.da.cf.qiso = S.dqiso.p;
         S.dA.upload(A);

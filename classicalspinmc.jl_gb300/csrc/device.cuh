@@ -72,8 +72,9 @@ template <typename R> struct Coef {
     // O+P (dE), O+P/2 (energy share), and the scalar of each bilinear slot
     // when every coupling is a multiple of the identity
     const R *A, *Q, *E2, *Js;
-    // per tensor id: isotropic cubic {flag, kappa}, quartic {flag, q1, q2, q3}
-    const R *ciso, *qiso;
+    // per tensor id: isotropic bilinear {flag, J}, cubic {flag, kappa},
+    // quartic {flag, q1, q2, q3}
+    const R *miso, *ciso, *qiso;
 };
 
 template <typename R> struct V3 {
@@ -169,8 +170,9 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     const int64_t Np = tb.Np;
     for (int t = 0; t < tb.W2; t++) {
         const int64_t j = tb.p2[t * Np + d];
-        const R *M = cf.mats + 9 * cf.c2[b * tb.W2 + t];
-        hb = add_matvec(hb, M, sv.get(j));
+        const int id = cf.c2[b * tb.W2 + t];
+        if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sv.get(j)); // J I
+        else hb = add_matvec(hb, cf.mats + 9 * id, sv.get(j));
     }
     if (CUB) {
         for (int t = 0; t < tb.W3; t++) {

@@ -302,18 +302,30 @@ static void assign_per_basis(Plan &P) {
     }
 }
 
-// The isotropic forms of the deduplicated cubic and quartic tensors (see
-// Plan::cub_iso): the only rotation-invariant rank-3 tensor is eps_abc, the
-// rank-4 ones are the three pairings of delta products.  A tensor is tagged
-// only if it equals the form entry by entry; the kernels then evaluate
-// kappa (s_j x s_k) and q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k)
-// instead of the dense contraction.
+// The isotropic forms of the deduplicated coupling tensors (see
+// Plan::cub_iso): J times the identity for the bilinear matrices; the only
+// rotation-invariant rank-3 tensor is eps_abc, the rank-4 ones are the three
+// pairings of delta products.  A tensor is tagged only if it equals the form
+// entry by entry; the kernels then evaluate J s_j, kappa (s_j x s_k) and
+// q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k) instead of the dense
+// contraction.
 static void classify_isotropic(Plan &P) {
     auto eps = [](int a, int b, int c) {
         if (a == b || b == c || a == c) return 0;
         return ((a + 1) % 3 == b) ? 1 : -1; // (0,1,2) and its cyclic shifts: +1
     };
-    const size_t nc = P.cubs.size() / 27, nq = P.quas.size() / 81;
+    const size_t nm = P.mats.size() / 9, nc = P.cubs.size() / 27, nq = P.quas.size() / 81;
+    P.mat_iso.assign(2 * nm, 0.0);
+    for (size_t t = 0; t < nm; t++) {
+        const double *M = &P.mats[9 * t];
+        bool ok = true;
+        for (int k = 0; k < 9; k++)
+            if (M[k] != (k % 4 == 0 ? M[0] : 0.0)) ok = false;
+        if (ok) {
+            P.mat_iso[2 * t] = 1.0;
+            P.mat_iso[2 * t + 1] = M[0];
+        }
+    }
     P.cub_iso.assign(2 * nc, 0.0);
     for (size_t t = 0; t < nc; t++) {
         const double *C = &P.cubs[27 * t];

@@ -65,6 +65,8 @@ struct Plan {
     // qua_iso {1, q1, q2, q3} when R[a,b,c,d] = q1 d_ab d_cd + q2 d_ac d_bd +
     // q3 d_ad d_bc (exactly); {0, ...} otherwise
     std::vector<double> cub_iso, qua_iso;
+    // mat_iso {1, J} when a bilinear matrix is J times the identity
+    std::vector<double> mat_iso;
     // colouring and device order
     int n_colours = 0;
     std::vector<int32_t> colour_of;  // reference order
