@@ -2,6 +2,8 @@
 // colour-sweep kernels (kernels.cu) and the replay kernel (exact.cu).
 #pragma once
 
+#include <type_traits>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -164,75 +166,114 @@ __host__ __device__ __forceinline__ Spins<double> spins_of(double *base, int64_t
 template <typename R, typename Idx, bool CUB, bool QUA, class SV>
 __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b,
                                                V3<R> &hb, V3<R> &hc, V3<R> &hq) {
+    using F = Fp<R>;
     hb = {R(0), R(0), R(0)};
     hc = {R(0), R(0), R(0)};
     hq = {R(0), R(0), R(0)};
     const int64_t Np = tb.Np;
-    for (int t = 0; t < tb.W2; t++) {
-        const int64_t j = tb.p2[t * Np + d];
+    // one term of each kind, its partner spins given
+    auto bil = [&](int t, V3<R> sj) {
         const int id = cf.c2[b * tb.W2 + t];
-        if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sv.get(j)); // J I
-        else hb = add_matvec(hb, cf.mats + 9 * id, sv.get(j));
-    }
-    if (CUB) {
-        for (int t = 0; t < tb.W3; t++) {
-            const int64_t j = tb.p3[(2 * t) * Np + d], k = tb.p3[(2 * t + 1) * Np + d];
-            const int id = cf.c3[b * tb.W3 + t];
-            const V3<R> sj = sv.get(j), sk = sv.get(k);
-            using F = Fp<R>;
-            if (cf.ciso[2 * id] != R(0)) { // kappa eps_abc: kappa (s_j x s_k)
-                const R kap = cf.ciso[2 * id + 1];
-                const V3<R> x = {F::fma(sj.y, sk.z, -F::mul(sj.z, sk.y)), F::fma(sj.z, sk.x, -F::mul(sj.x, sk.z)),
-                                 F::fma(sj.x, sk.y, -F::mul(sj.y, sk.x))};
-                hc = add_scaled(hc, kap, x);
-                continue;
-            }
-            const R *C = cf.cubs + 27 * id;
-            const R a0 = sj.x, a1 = sj.y, a2 = sj.z, b0 = sk.x, b1 = sk.y, b2 = sk.z;
-            const R o[9] = {F::mul(a0, b0), F::mul(a0, b1), F::mul(a0, b2), F::mul(a1, b0), F::mul(a1, b1),
-                            F::mul(a1, b2), F::mul(a2, b0), F::mul(a2, b1), F::mul(a2, b2)};
-            R sx = 0, sy = 0, sz = 0;
-#pragma unroll
-            for (int q = 0; q < 9; q++) {
-                sx = F::fma(C[q], o[q], sx);
-                sy = F::fma(C[9 + q], o[q], sy);
-                sz = F::fma(C[18 + q], o[q], sz);
-            }
-            hc = vadd(hc, V3<R>{sx, sy, sz});
+        if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sj); // J I
+        else hb = add_matvec(hb, cf.mats + 9 * id, sj);
+    };
+    auto cub = [&](int t, V3<R> sj, V3<R> sk) {
+        const int id = cf.c3[b * tb.W3 + t];
+        if (cf.ciso[2 * id] != R(0)) { // kappa eps_abc: kappa (s_j x s_k)
+            const R kap = cf.ciso[2 * id + 1];
+            const V3<R> x = {F::fma(sj.y, sk.z, -F::mul(sj.z, sk.y)), F::fma(sj.z, sk.x, -F::mul(sj.x, sk.z)),
+                             F::fma(sj.x, sk.y, -F::mul(sj.y, sk.x))};
+            hc = add_scaled(hc, kap, x);
+            return;
         }
+        const R *C = cf.cubs + 27 * id;
+        const R a0 = sj.x, a1 = sj.y, a2 = sj.z, b0 = sk.x, b1 = sk.y, b2 = sk.z;
+        const R o[9] = {F::mul(a0, b0), F::mul(a0, b1), F::mul(a0, b2), F::mul(a1, b0), F::mul(a1, b1),
+                        F::mul(a1, b2), F::mul(a2, b0), F::mul(a2, b1), F::mul(a2, b2)};
+        R sx = 0, sy = 0, sz = 0;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            sx = F::fma(C[q], o[q], sx);
+            sy = F::fma(C[9 + q], o[q], sy);
+            sz = F::fma(C[18 + q], o[q], sz);
+        }
+        hc = vadd(hc, V3<R>{sx, sy, sz});
+    };
+    auto qua = [&](int t, V3<R> sj, V3<R> sk, V3<R> sl) {
+        const int id = cf.c4[b * tb.W4 + t];
+        if (cf.qiso[4 * id] != R(0)) { // q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k)
+            const R w1 = F::mul(cf.qiso[4 * id + 1], dot(sk, sl)), w2 = F::mul(cf.qiso[4 * id + 2], dot(sj, sl)),
+                    w3 = F::mul(cf.qiso[4 * id + 3], dot(sj, sk));
+            hq = add_scaled(add_scaled(add_scaled(hq, w1, sj), w2, sk), w3, sl);
+            return;
+        }
+        const R *Q = cf.quas + 81 * id;
+        const R a[3] = {sj.x, sj.y, sj.z}, bb[3] = {sk.x, sk.y, sk.z}, c[3] = {sl.x, sl.y, sl.z};
+        R sx = 0, sy = 0, sz = 0;
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                const R ab = F::mul(a[p], bb[q]);
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+                    const R o = F::mul(ab, c[r]);
+                    const int idx = (p * 3 + q) * 3 + r;
+                    sx = F::fma(Q[idx], o, sx);
+                    sy = F::fma(Q[27 + idx], o, sy);
+                    sz = F::fma(Q[54 + idx], o, sz);
+                }
+            }
+        hq = vadd(hq, V3<R>{sx, sy, sz});
+    };
+    // Spins in global memory: terms in groups (bilinear threes, cubic and
+    // quartic pairs), the group's partner indices and then its partner spins
+    // loaded before any is used (several gathers in flight per dependent
+    // step instead of one); same arithmetic order.
+    constexpr bool kPairs = std::is_same<SV, Spins<R>>::value;
+    int t = 0;
+    if (kPairs) { // bilinear terms in threes
+        constexpr int G = 3;
+        for (; t + G <= tb.W2; t += G) {
+            int64_t j[G];
+            V3<R> sj[G];
+#pragma unroll
+            for (int u = 0; u < G; u++) j[u] = tb.p2[(t + u) * Np + d];
+#pragma unroll
+            for (int u = 0; u < G; u++) sj[u] = sv.get(j[u]);
+#pragma unroll
+            for (int u = 0; u < G; u++) bil(t + u, sj[u]);
+        }
+    }
+    for (; t < tb.W2; t++) bil(t, sv.get(tb.p2[t * Np + d]));
+    if (CUB) {
+        t = 0;
+        if (kPairs)
+            for (; t + 2 <= tb.W3; t += 2) {
+                const int64_t j0 = tb.p3[(2 * t) * Np + d], k0 = tb.p3[(2 * t + 1) * Np + d];
+                const int64_t j1 = tb.p3[(2 * t + 2) * Np + d], k1 = tb.p3[(2 * t + 3) * Np + d];
+                const V3<R> sj0 = sv.get(j0), sk0 = sv.get(k0), sj1 = sv.get(j1), sk1 = sv.get(k1);
+                cub(t, sj0, sk0);
+                cub(t + 1, sj1, sk1);
+            }
+        for (; t < tb.W3; t++) cub(t, sv.get(tb.p3[(2 * t) * Np + d]), sv.get(tb.p3[(2 * t + 1) * Np + d]));
     }
     if (QUA) {
-        for (int t = 0; t < tb.W4; t++) {
-            const int64_t j = tb.p4[(3 * t) * Np + d], k = tb.p4[(3 * t + 1) * Np + d], l = tb.p4[(3 * t + 2) * Np + d];
-            const int id = cf.c4[b * tb.W4 + t];
-            const V3<R> sj = sv.get(j), sk = sv.get(k), sl = sv.get(l);
-            if (cf.qiso[4 * id] != R(0)) { // q1 s_j (s_k.s_l) + q2 s_k (s_j.s_l) + q3 s_l (s_j.s_k)
-                using F = Fp<R>;
-                const R w1 = F::mul(cf.qiso[4 * id + 1], dot(sk, sl)), w2 = F::mul(cf.qiso[4 * id + 2], dot(sj, sl)),
-                        w3 = F::mul(cf.qiso[4 * id + 3], dot(sj, sk));
-                hq = add_scaled(add_scaled(add_scaled(hq, w1, sj), w2, sk), w3, sl);
-                continue;
+        t = 0;
+        if (kPairs)
+            for (; t + 2 <= tb.W4; t += 2) {
+                const int64_t j0 = tb.p4[(3 * t) * Np + d], k0 = tb.p4[(3 * t + 1) * Np + d],
+                              l0 = tb.p4[(3 * t + 2) * Np + d];
+                const int64_t j1 = tb.p4[(3 * t + 3) * Np + d], k1 = tb.p4[(3 * t + 4) * Np + d],
+                              l1 = tb.p4[(3 * t + 5) * Np + d];
+                const V3<R> sj0 = sv.get(j0), sk0 = sv.get(k0), sl0 = sv.get(l0);
+                const V3<R> sj1 = sv.get(j1), sk1 = sv.get(k1), sl1 = sv.get(l1);
+                qua(t, sj0, sk0, sl0);
+                qua(t + 1, sj1, sk1, sl1);
             }
-            const R *Q = cf.quas + 81 * id;
-            const R a[3] = {sj.x, sj.y, sj.z}, bb[3] = {sk.x, sk.y, sk.z}, c[3] = {sl.x, sl.y, sl.z};
-            using F = Fp<R>;
-            R sx = 0, sy = 0, sz = 0;
-#pragma unroll
-            for (int p = 0; p < 3; p++)
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    const R ab = F::mul(a[p], bb[q]);
-#pragma unroll
-                    for (int r = 0; r < 3; r++) {
-                        const R o = F::mul(ab, c[r]);
-                        const int idx = (p * 3 + q) * 3 + r;
-                        sx = F::fma(Q[idx], o, sx);
-                        sy = F::fma(Q[27 + idx], o, sy);
-                        sz = F::fma(Q[54 + idx], o, sz);
-                    }
-                }
-            hq = vadd(hq, V3<R>{sx, sy, sz});
-        }
+        for (; t < tb.W4; t++)
+            qua(t, sv.get(tb.p4[(3 * t) * Np + d]), sv.get(tb.p4[(3 * t + 1) * Np + d]),
+                sv.get(tb.p4[(3 * t + 2) * Np + d]));
     }
 }
 
