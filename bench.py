@@ -344,6 +344,11 @@ def other_workload(name, m):
         Ts = np.exp(np.linspace(math.log(0.05), math.log(1.5), 32))
         return ([lat], [32], Ts, "fp32", dict(or_rate=5, swap_rate=10, probe_rate=10, iters=10),
                 f"pyrochlore J1 + cubic + quartic, shape {shape} ({lat.size} sites), 32 PT replicas, FP32")
+    if name == "sc_large_fp32":  # replicas beyond shared memory and beyond L2: the global sweeps from HBM
+        lat = m.Lattice((64, 64, 64), E.sc_heisenberg(J=1.0, D=0.2), 1.0, initialCondition="none")
+        Ts = np.exp(np.linspace(math.log(0.1), math.log(2.0), 64))
+        return ([lat], [64], Ts, "fp32", dict(or_rate=5, swap_rate=10, probe_rate=10, iters=10),
+                "simple cubic L=64 (262144 sites), 64 PT replicas (268 MB of spins), FP32, global colour sweeps")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -410,6 +415,19 @@ def bench_other(args):
     value = upd * args.steps / t_dev
     cl = C.c_int32()
     ctx.call("csmc_cluster_size", C.byref(cl))
+    # algorithmic bytes s_b (2 + z) per update against the measured HBM copy
+    # bandwidth; with the working set inside L2 the figure is the rate a
+    # streaming kernel would need, not DRAM traffic
+    z = max(l.info.width_bilinear for l in lats)
+    s_b = 12 if prec == "fp32" else 24
+    ws = sum(l.info.padded_sites * r for l, r in zip(lats, reps)) * (16 if prec == "fp32" else 24)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    ach = upd * args.steps * s_b * (2 + z) / t_dev / 1e9
+    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+            "kernel": "whole step (every launch)", "bytes_per_update": s_b * (2 + z),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+            "working_set_bytes": ws, "working_set_in_l2": ws < 126 * 2**20}
     line = {"metric": "site updates/s (Metropolis+OR)", "value": value, "unit": "site updates/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -417,7 +435,7 @@ def bench_other(args):
             "config": {"workload": args.workload, "description": desc, "site_updates_per_step": upd,
                        "ctas_per_replica": cl.value, "l2": "flushed between steps (256 MB write)",
                        "autotune_candidates": tuned},
-            "clocks": clk.summary(), "gpu_launches": launches}
+            "roofline": roof, "clocks": clk.summary(), "gpu_launches": launches}
     print(json.dumps(line))
 
 
@@ -474,7 +492,7 @@ def main():
                     help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",
                     choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
-                             "pyrochlore_large_fp32", "structure_factor"],
+                             "pyrochlore_large_fp32", "sc_large_fp32", "structure_factor"],
                     help="sc_pt (default): the 64-replica simple-cubic line; the others measure the remaining "
                          "configurations (device throughput only)")
     args = ap.parse_args()
