@@ -18,12 +18,17 @@ namespace csmc {
 
 static thread_local std::string g_err;
 
+// A failed runtime call throws; the runtime's last-error slot is read (and so
+// cleared) first, so that a recoverable failure such as an allocation that
+// does not fit is not reported again by a later, unrelated check.
 #define CK(call)                                                                                                       \
     do {                                                                                                               \
         cudaError_t e_ = (call);                                                                                       \
-        if (e_ != cudaSuccess)                                                                                         \
+        if (e_ != cudaSuccess) {                                                                                       \
+            (void)cudaGetLastError();                                                                                  \
             throw Error(e_ == cudaErrorMemoryAllocation ? CSMC_ERR_OOM : CSMC_ERR_CUDA,                                \
                         std::string(#call) + ": " + cudaGetErrorString(e_));                                           \
+        }                                                                                                              \
     } while (0)
 
 static void require(bool ok, int code, const std::string &msg) {

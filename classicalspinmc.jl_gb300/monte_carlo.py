@@ -238,6 +238,7 @@ class MonteCarlo:
         self.momentum_vectors = None if ks is None else np.asfortranarray(ks, dtype=np.float64)
         self.accepted = np.zeros(R)
         self.exchanged = np.zeros(R)
+        self.initial_configurations = {}  # parallel_tempering(saveIC=...): {rank: {timestep: spins}}
 
     # -- state --------------------------------------------------------------
     @property
@@ -429,6 +430,10 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
 
     Like the reference, report_interval and checkpoint_rate must be nonzero
     (``sweep % 0`` throws a DivideError at monte_carlo.jl:355 and :383).
+    ``saveIC`` lists ranks (slots) whose configuration is saved at every
+    checkpoint of the measurement phase (monte_carlo.jl:353-364); the
+    configurations are kept in ``mc.initial_configurations[rank][timestep]``
+    (3 x N arrays) instead of ``IC_<rank>/IC_<timestep>.h5`` files.
     Returns the per-replica energy and |M| series and the derived observables.
     """
     alg = Metropolis() if alg is None else alg
@@ -447,14 +452,21 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     Es, Ms = [], []
     start = 0
 
+    save = sorted({int(r) for r in saveIC})
+    if any(r < 0 or r >= R for r in save):
+        raise ValueError(f"saveIC ranks must be in 0..{R - 1}")
+
+    def is_corr(it):  # correlations at the probe, after the exchange (monte_carlo.jl:371-375)
+        return mc.corr and p.probe_rate > 0 and it >= p.t_thermalization and it % p.probe_rate == 0
+
+    def is_ic(it):  # initial configurations at the checkpoints of the measurement (monte_carlo.jl:353-364)
+        return bool(save) and it >= p.t_thermalization and it % p.checkpoint_rate == 0
+
     def pieces(a, b):
-        """[a, b) split after every probe iteration when correlations are measured
-        (monte_carlo.jl:371-375 computes them at the probe, after the exchange)."""
-        if not mc.corr or p.probe_rate <= 0:
-            return [(a, b)]
+        """[a, b) split after every iteration whose end state is read on the host."""
         out, q = [], a
         for it in range(a, b):
-            if it >= p.t_thermalization and it % p.probe_rate == 0:
+            if is_corr(it) or is_ic(it):
                 out.append((q, it + 1))
                 q = it + 1
         if q < b:
@@ -469,10 +481,14 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
             k, E_, M_ = _run_piece(mc, a, b - a, alg, resident_block, acc, exc)
             Es.append(E_[:k])
             Ms.append(M_[:k])
-            if mc.corr and b - 1 >= p.t_thermalization and p.probe_rate > 0 and (b - 1) % p.probe_rate == 0:
+            if is_corr(b - 1):
                 ssf = structure_factors(mc, mc.momentum_vectors)
                 for r in range(R):
                     mc.observables[r].push_correlations(ssf[r])
+            if is_ic(b - 1):  # write_initial_configuration of IC_<rank>/IC_<timestep>, kept in memory
+                timestep = (b - 1 - p.t_thermalization) // p.checkpoint_rate
+                for r in save:
+                    mc.initial_configurations.setdefault(r, {})[timestep] = mc.spins(r)
         mc.accepted += acc
         mc.exchanged += exc
         start += n

@@ -84,3 +84,26 @@ def test_parallel_tempering_measures_correlations_at_every_probe(m, orc, precisi
         trace0 = samples[:, 0, 0] + samples[:, 4, 0] + samples[:, 8, 0]
         rel = 1e-4 if precision == "fp32" else 1e-10
         assert np.allclose(trace0, out["magnetization"][:, r] ** 2 / lat.size, rtol=rel, atol=rel)
+
+
+def test_parallel_tempering_saves_initial_configurations(m, orc):
+    """saveIC (monte_carlo.jl:353-364): at every checkpoint of the measurement
+    phase the listed ranks' configurations are kept; each equals the
+    configuration the probe of the same iteration measured."""
+    uc = m.examples.triangular_afm(h=0.3)
+    lat = m.Lattice((6, 6), uc, 1.0)
+    ol = orc.OracleLattice(uc, (6, 6), 1.0)
+    mc = m.MonteCarlo([0.2, 0.4, 0.9], lat, {"overrelaxation_rate": 5}, precision="fp64", seed=4)
+    p = mc.parameters
+    p.t_thermalization, p.t_measurement, p.report_interval, p.checkpoint_rate = 10, 30, 15, 10
+    p.probe_rate, p.swap_rate = 5, 5
+    out = m.parallel_tempering(mc, saveIC=(0, 2), verbose=False)
+    ics = mc.initial_configurations
+    assert sorted(ics) == [0, 2]
+    for r in (0, 2):
+        assert sorted(ics[r]) == [0, 1, 2]  # iterations 10, 20, 30
+        for ts in range(3):
+            k = 2 * ts  # probes at 10, 15, 20, ...
+            s = ics[r][ts]
+            assert ol.total_energy(s) == pytest.approx(out["energy"][k, r], rel=1e-12, abs=1e-12)
+            assert ol.magnetization(s) == pytest.approx(out["magnetization"][k, r], rel=1e-12, abs=1e-12)

@@ -32,3 +32,16 @@ def test_selftest_rejects_unknown_waits(m):
     lat = m.Lattice((4, 4), m.examples.square_heisenberg(), 1.0)
     mc = m.MonteCarlo(0.5, lat, {}, precision="fp64", seed=1)
     assert m.lib().csmc_selftest_timeout(mc.ctx.handle, 7) == 1
+
+
+def test_device_allocation_failure_is_an_error_code(m):
+    """A context whose replicas cannot fit (131072 replicas of 262144 sites:
+    550 GB of spins on a 288 GB device) fails with CSMC_ERR_OOM, frees what it
+    had allocated, and the device stays usable."""
+    big = m.Lattice((64, 64, 64), m.examples.sc_heisenberg(), 1.0, initialCondition="none")
+    with pytest.raises(m.CSMCError) as e:
+        m.monte_carlo.Context([big], [131072], precision="fp32", seed=1)
+    assert e.value.code == 2  # CSMC_ERR_OOM
+    lat = m.Lattice((8, 8), m.examples.square_heisenberg(), 1.0)
+    mc = m.MonteCarlo(0.5, lat, {"overrelaxation_rate": 5}, precision="fp32", seed=2)
+    assert 0 <= m.Metropolis()(mc, 0.5) <= lat.size
