@@ -94,12 +94,14 @@ template <> struct Fp<float> {
     static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
     static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
     static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 };
 template <> struct Fp<double> {
     static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
     static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
     static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
 };
 // acc + M s, one fused multiply-add per term in the order M[0] s.x, M[1] s.y,
 // M[2] s.z (a matrix c*I gives exactly acc + c s)
@@ -315,21 +317,23 @@ __device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn
 }
 
 // Contribution of site d to total_energy (hamiltonian.jl:70-132):
-// -s.h + s.O.s + (s.hb + s.P.s)/2 + s.hc/3 + s.hq/4.
+// -s.h + s.O.s + (s.hb + s.P.s)/2 + s.hc/3 + s.hq/4, in the arithmetic type R.
+// Callers add a few sites' shares in R per thread and sum those partials in
+// FP64 (on this device FP64 runs at a small fraction of the FP32 rate, and a
+// per-site FP64 sum made the energy kernels FP64-bound).
 template <typename R, typename Idx, bool CUB, bool QUA, class SV>
-__device__ __forceinline__ double site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d,
-                                                    int b) {
-    using F = Fp<double>;
+__device__ __forceinline__ R site_energy_share(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b) {
+    using F = Fp<R>;
     V3<R> hb, hc, hq;
     partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
     const V3<R> s = sv.get(d);
     const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
-    const double eo = (double)dot(s, matvec(cf.O + 9 * b, s));
-    const double ep = (double)dot(s, matvec(cf.P + 9 * b, s));
-    const double ez = (double)dot(s, h);
-    double e = F::add(F::sub(eo, ez), F::mul(0.5, F::add((double)dot(s, hb), ep)));
-    if (CUB) e = F::add(e, (double)dot(s, hc) / 3.0);
-    if (QUA) e = F::fma(0.25, (double)dot(s, hq), e);
+    const R eo = dot(s, matvec(cf.O + 9 * b, s));
+    const R ep = dot(s, matvec(cf.P + 9 * b, s));
+    const R ez = dot(s, h);
+    R e = F::add(F::sub(eo, ez), F::mul(R(0.5), F::add(dot(s, hb), ep)));
+    if (CUB) e = F::add(e, F::div(dot(s, hc), R(3)));
+    if (QUA) e = F::fma(R(0.25), dot(s, hq), e);
     return e;
 }
 

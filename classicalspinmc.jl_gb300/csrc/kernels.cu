@@ -156,19 +156,24 @@ __global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, 
     p.set(d, {-H.x / n * a.S, -H.y / n * a.S, -H.z / n * a.S});
 }
 
+// The reductions give each thread RK sites (stride GB) of a block's RB = GB x
+// RK: the thread sums them in R, the block sums the threads' partials in FP64.
+constexpr int RK = 8, RB = GB * RK;
+
 // Per-block partial sums of total_energy (hamiltonian.jl:70-132).
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, double *part) {
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
-    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
-    double e = 0.0;
-    if (d < a.tb.Np && a.dev2ref[d] >= 0) {
-        const int b = a.tb.pat[d];
-        e = site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
+    R acc = R(0);
+#pragma unroll 1
+    for (int k = 0; k < RK; k++) {
+        const int64_t d = (int64_t)blockIdx.x * RB + k * GB + threadIdx.x;
+        if (d < a.tb.Np && a.dev2ref[d] >= 0)
+            acc = Fp<R>::add(acc, site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, a.tb.pat[d]));
     }
-    e = block_sum<GB>(e, scratch);
+    const double e = block_sum<GB>((double)acc, scratch);
     if (threadIdx.x == 0) part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = e;
 }
 
@@ -177,14 +182,18 @@ template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArg
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
-    const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
-    double mx = 0, my = 0, mz = 0;
-    if (d < a.tb.Np) { // padding holds zero spins
-        const V3<R> s = p.get(d);
-        mx = s.x;
-        my = s.y;
-        mz = s.z;
+    R ax = R(0), ay = R(0), az = R(0);
+#pragma unroll 2
+    for (int k = 0; k < RK; k++) {
+        const int64_t d = (int64_t)blockIdx.x * RB + k * GB + threadIdx.x;
+        if (d < a.tb.Np) { // padding holds zero spins
+            const V3<R> s = p.get(d);
+            ax = Fp<R>::add(ax, s.x);
+            ay = Fp<R>::add(ay, s.y);
+            az = Fp<R>::add(az, s.z);
+        }
     }
+    double mx = ax, my = ay, mz = az;
     mx = block_sum<GB>(mx, scratch);
     my = block_sum<GB>(my, scratch);
     mz = block_sum<GB>(mz, scratch);
@@ -388,13 +397,13 @@ void launch_det_colour(const SysArgs<R> &a, int64_t start, int64_t count, int ch
     DISPATCH_CQ(a, k_det_colour, <<<g, GB, 0, st>>>(a, start, count, chain_lo));
 }
 
-int64_t partial_blocks(int64_t Np) { return (Np + GB - 1) / GB; }
+int64_t partial_blocks(int64_t Np) { return (Np + RB - 1) / RB; }
 
 template <typename R>
 void launch_energy(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
                    cudaStream_t st) {
     if (n_chains <= 0) return;
-    dim3 g = grid_for<R>(a.tb.Np, n_chains);
+    const dim3 g((unsigned)partial_blocks(a.tb.Np), (unsigned)n_chains);
     DISPATCH_CQ(a, k_energy_part, <<<g, GB, 0, st>>>(a, chain_lo, part));
     k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 1, cs.E_chain, a.chain_base, chain_lo);
 }
@@ -403,7 +412,7 @@ template <typename R>
 void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int n_chains, double *part,
                    cudaStream_t st) {
     if (n_chains <= 0) return;
-    dim3 g = grid_for<R>(a.tb.Np, n_chains);
+    const dim3 g((unsigned)partial_blocks(a.tb.Np), (unsigned)n_chains);
     k_magnet_part<R><<<g, GB, 0, st>>>(a, chain_lo, part);
     k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 3, cs.M_chain, a.chain_base, chain_lo);
 }

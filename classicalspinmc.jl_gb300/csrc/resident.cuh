@@ -296,17 +296,20 @@ template <typename R, int CL> struct ResidentCommon {
         return CL == 1 ? i : S.src_start[rank][col] + (i - S.loc_start[rank][col]);
     }
 
+    // |sum_i s_i|: each thread adds its sites in R, the block and the cluster
+    // add the threads' partials in FP64
     __device__ double magnetization() const { // valid in thread 0
-        double mx = 0, my = 0, mz = 0;
+        R ax = R(0), ay = R(0), az = R(0);
         for (int col = 0; col < S.n_colours; col++) { // the sites of this CTA only
             const int st = col_begin(col), n = col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const V3<R> s = sp.get(st + i);
-                mx += s.x;
-                my += s.y;
-                mz += s.z;
+                ax = Fp<R>::add(ax, s.x);
+                ay = Fp<R>::add(ay, s.y);
+                az = Fp<R>::add(az, s.z);
             }
         }
+        double mx = ax, my = ay, mz = az;
         sy.sum3(mx, my, mz);
         return sqrt(mx * mx + my * my + mz * mz);
     }
@@ -417,16 +420,16 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
         }
     }
 
-    __device__ double energy() const { // valid in thread 0
-        double e = 0.0;
+    __device__ double energy() const { // valid in thread 0; per-thread partials in R, their sum in FP64
+        R acc = R(0);
         for (int col = 0; col < S.n_colours; col++) {
             const int st = this->col_begin(col), n = this->col_size(col);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int d = st + i;
-                e += site_energy_share<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, tb.pat[d]);
+                acc = Fp<R>::add(acc, site_energy_share<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, tb.pat[d]));
             }
         }
-        return this->sy.sum(e);
+        return this->sy.sum((double)acc);
     }
 };
 
@@ -624,8 +627,8 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         return acc;
     }
 
-    __device__ double energy() const { // valid in thread 0
-        double e = 0.0;
+    __device__ double energy() const { // valid in thread 0; per-thread partials in R, their sum in FP64
+        R acc = R(0);
         for (int col = 0; col < S.n_colours; col++) {
             R J[W], m[9];
             V3<R> h;
@@ -638,11 +641,11 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 wn = next_word(st, n, k);
                 const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
-                const double part = (double)Fp<R>::sub(dot(s, onsite(m, s)), dot(s, h));
-                e = Fp<double>::add(e, Fp<double>::fma(0.5, (double)dot(s, hb), part));
+                const R part = Fp<R>::sub(dot(s, onsite(m, s)), dot(s, h));
+                acc = Fp<R>::add(acc, Fp<R>::fma(R(0.5), dot(s, hb), part));
             }
         }
-        return this->sy.sum(e);
+        return this->sy.sum((double)acc);
     }
 };
 

@@ -69,6 +69,13 @@ def setup(m, orc, name, precision, R=1, seed=20261203, T=1.0):
     return lat, ol, mc
 
 
+def obs_tol(precision):
+    """Per-site tolerance of energies and |M| between launch configurations:
+    single precision adds each thread's sites in FP32 before the FP64 sum, and
+    the split of sites over threads differs between configurations."""
+    return 1e-9 if precision == "fp64" else 1e-6
+
+
 def term_scale(lat):
     """Per-site sum of |coefficients| (|s| = 1): bounds sum|terms| of the local field."""
     t = lat.tables()
@@ -499,7 +506,7 @@ def test_cluster_sizes_give_the_same_chain(m, orc, name, precision):
                     mc.accepted.copy(), mc.exchanged.copy(), np.atleast_1d(mc.sigma)))
     for other in res[1:]:
         assert np.abs(res[0][0] - other[0]).max() <= 1e-12 * (1 if precision == "fp64" else 1e6)
-        assert np.abs(res[0][1] - other[1]).max() <= 1e-9 * lat.size
-        assert np.abs(res[0][2] - other[2]).max() <= 1e-9 * lat.size
+        assert np.abs(res[0][1] - other[1]).max() <= obs_tol(precision) * lat.size
+        assert np.abs(res[0][2] - other[2]).max() <= obs_tol(precision) * lat.size
         assert np.array_equal(res[0][3], other[3]) and np.array_equal(res[0][4], other[4])
         assert np.allclose(res[0][5], other[5], rtol=1e-12)
