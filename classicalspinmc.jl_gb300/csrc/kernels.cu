@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, 
 }
 
 // The reductions give each thread RK sites (stride GB) of a block's RB = GB x
-// RK: the thread sums them in R, the block sums the threads' partials in FP64.
+// RK: the thread and then its warp sum them in R, the block sums the warps'
+// partials in FP64.
 constexpr int RK = 8, RB = GB * RK;
 
 // Per-block partial sums of total_energy (hamiltonian.jl:70-132).
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, 
         if (d < a.tb.Np && a.dev2ref[d] >= 0)
             acc = Fp<R>::add(acc, site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, a.tb.pat[d]));
     }
-    const double e = block_sum<GB>((double)acc, scratch);
+    const double e = block_sum<GB>(acc, scratch);
     if (threadIdx.x == 0) part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = e;
 }
 
@@ -193,10 +194,7 @@ template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArg
             az = Fp<R>::add(az, s.z);
         }
     }
-    double mx = ax, my = ay, mz = az;
-    mx = block_sum<GB>(mx, scratch);
-    my = block_sum<GB>(my, scratch);
-    mz = block_sum<GB>(mz, scratch);
+    const double mx = block_sum<GB>(ax, scratch), my = block_sum<GB>(ay, scratch), mz = block_sum<GB>(az, scratch);
     if (threadIdx.x == 0) {
         int64_t o = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * 3;
         part[o] = mx;

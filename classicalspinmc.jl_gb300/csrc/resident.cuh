@@ -242,7 +242,7 @@ template <int CL> struct Sync {
             __syncthreads();
         }
     }
-    __device__ double sum(double v) const {
+    template <typename T> __device__ double sum(T v) const {
         double t = block_sum_any(v, scratch);
         if (CL == 1) return t;
         if (threadIdx.x == 0) red[0] = t;
@@ -253,10 +253,10 @@ template <int CL> struct Sync {
         cluster_sync_all();
         return tot;
     }
-    __device__ void sum3(double &a, double &b, double &c) const {
-        a = block_sum_any(a, scratch);
-        b = block_sum_any(b, scratch);
-        c = block_sum_any(c, scratch);
+    template <typename T> __device__ void sum3(T x, T y, T z, double &a, double &b, double &c) const {
+        a = block_sum_any(x, scratch);
+        b = block_sum_any(y, scratch);
+        c = block_sum_any(z, scratch);
         if (CL == 1) return;
         if (threadIdx.x == 0) {
             red[0] = a;
@@ -309,8 +309,8 @@ template <typename R, int CL> struct ResidentCommon {
                 az = Fp<R>::add(az, s.z);
             }
         }
-        double mx = ax, my = ay, mz = az;
-        sy.sum3(mx, my, mz);
+        double mx, my, mz;
+        sy.sum3(ax, ay, az, mx, my, mz);
         return sqrt(mx * mx + my * my + mz * mz);
     }
 
@@ -429,7 +429,7 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
                 acc = Fp<R>::add(acc, site_energy_share<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, tb.pat[d]));
             }
         }
-        return this->sy.sum((double)acc);
+        return this->sy.sum(acc);
     }
 };
 
@@ -645,7 +645,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 acc = Fp<R>::add(acc, Fp<R>::fma(R(0.5), dot(s, hb), part));
             }
         }
-        return this->sy.sum((double)acc);
+        return this->sy.sum(acc);
     }
 };
 
@@ -817,7 +817,7 @@ __global__ void __launch_bounds__(NT, 1)
                     const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
                     msweep++;
                     sweeps++;
-                    const double at = sync.sum((double)a);
+                    const double at = sync.sum(a); // exact: an integer sum per warp
                     if (threadIdx.x == 0) {
                         acc_total += at;
                         if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) { // metropolis.jl:124-126
