@@ -32,7 +32,15 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
     const Spins<R> p = replica(a, r);
     const int slot = cs.slot_of[c];
     const double T = T_override > 0 ? T_override : cs.T_slot[slot];
-    const R sigma = (R)cs.sigma_slot[slot];
+    // 1/T and sigma in R, formed once per block: FP64 division runs at a
+    // small fraction of the FP32 rate on this device
+    __shared__ R s_invT, s_sigma;
+    if (threadIdx.x == 0) {
+        s_invT = (R)(1.0 / T);
+        s_sigma = (R)cs.sigma_slot[slot];
+    }
+    __syncthreads();
+    const R invT = s_invT, sigma = s_sigma;
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
     unsigned acc = 0;
     if (i < count) {
@@ -46,7 +54,7 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
         const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
         bool accept = dE < R(0);
-        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(boltz_arg(dE, (R)(1.0 / T), T));
+        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
         if (accept) {
             p.set(d, sn);
             acc = 1;
