@@ -119,6 +119,19 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def job_throughput(t_rank_s, updates_per_rank, world, dist, device):
+    """Whole-job site updates/s of N independent replica sets (one per rank):
+    every rank did `updates_per_rank` in `t_rank_s` seconds; the job took the
+    slowest rank's time.  Returns (updates/s, that time)."""
+    t = t_rank_s
+    if dist:
+        import torch
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    return world * updates_per_rank / t, t
+
+
 def run_params(L, start, n, rec_E=None, rec_M=None, cap=0, path=None):
     path = RUN_PATH if path is None else path
     rp = L.RunParams()
@@ -200,12 +213,7 @@ def bench_ours(args, rank, world, dist):
             kern_launches += d
         barrier()
         wall = time.perf_counter() - t0
-    t_dev = dev_ms / 1e3
-    if dist:
-        tt = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(tt.item())
-    value = world * upd * args.steps / t_dev
+    value, t_dev = job_throughput(dev_ms / 1e3, upd * args.steps, world, dist, "cuda")
     out = {"value": value, "ms_per_step": 1e3 * t_dev / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
            "gpu_launches": launches, "clocks": clk.summary(), "ctas_per_replica": ranks.value, "autotune": tuned}
     # roofline of the dominant kernel (the resident sweep kernel, one launch per step)
