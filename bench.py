@@ -352,6 +352,12 @@ def other_workload(name, m):
         Ts = np.exp(np.linspace(math.log(0.05), math.log(1.5), 32))
         return ([lat], [32], Ts, "fp32", dict(or_rate=5, swap_rate=10, probe_rate=10, iters=10),
                 f"pyrochlore J1 + cubic + quartic, shape {shape} ({lat.size} sites), 32 PT replicas, FP32")
+    if name == "sc_constraint_fp32":  # MetropolisConstraintAdaptive: sequential proposals per replica
+        lat = m.Lattice((24, 24, 24), E.sc_heisenberg(J=1.0, D=0.2), 1.0, initialCondition="none")
+        Ts = np.exp(np.linspace(math.log(0.1), math.log(2.0), 64))
+        return ([lat], [64], Ts, "fp32", dict(or_rate=5, swap_rate=10, probe_rate=10, iters=10, kind=4),
+                "simple cubic L=24 (13824 sites), 64 PT replicas, MetropolisConstraintAdaptive with "
+                "c = M_z / N - 0.1 (weight 0.01), FP32, global path")
     if name == "sc_large_fp32":  # replicas beyond shared memory and beyond L2: the global sweeps from HBM
         lat = m.Lattice((64, 64, 64), E.sc_heisenberg(J=1.0, D=0.2), 1.0, initialCondition="none")
         Ts = np.exp(np.linspace(math.log(0.1), math.log(2.0), 64))
@@ -372,6 +378,12 @@ def bench_other(args):
     ctx.call("csmc_random_spins", C.c_uint64(SEED))
     if args.no_persistent:
         ctx.call("csmc_set_persistent", 0)
+    kind = kw.get("kind", L.METROPOLIS)
+    if kind >= L.METROPOLIS_CONSTRAINT:
+        k = L.ConstraintDesc()
+        k.g[2] = 1.0 / lats[0].size
+        k.c0, k.weight = -0.1, 0.01
+        ctx.call("csmc_set_constraint", 0, C.byref(k))
     sites = sum(l.size * r for l, r in zip(lats, reps))
     iters = kw["iters"]
     anneal = args.workload == "honeycomb_fp32"
@@ -386,7 +398,7 @@ def bench_other(args):
         rp = L.RunParams()
         rp.sweep_start, rp.n_sweeps, rp.t_thermalization = 1, 0, 0
         rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = kw["or_rate"], kw["swap_rate"], kw["probe_rate"]
-        rp.kind, rp.path = L.METROPOLIS, RUN_PATH
+        rp.kind, rp.path = kind, RUN_PATH
         entries = (L.TuneEntry * 16)()
         n = C.c_int32()
         ctx.call("csmc_autotune", C.byref(rp), 4, entries, 16, C.byref(n))
@@ -403,7 +415,7 @@ def bench_other(args):
             rp = L.RunParams()
             rp.sweep_start, rp.n_sweeps, rp.t_thermalization = it[0], iters, 0
             rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = kw["or_rate"], kw["swap_rate"], kw["probe_rate"]
-            rp.kind, rp.path = L.METROPOLIS, RUN_PATH
+            rp.kind, rp.path = kind, RUN_PATH
             ctx.call("csmc_run", C.byref(rp))
             it[0] += iters
         return stats(ctx)
@@ -500,7 +512,7 @@ def main():
                     help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",
                     choices=["sc_pt", "square_fp64", "honeycomb_fp32", "triangular_batch_fp32", "pyrochlore_fp32",
-                             "pyrochlore_large_fp32", "sc_large_fp32", "structure_factor"],
+                             "pyrochlore_large_fp32", "sc_large_fp32", "sc_constraint_fp32", "structure_factor"],
                     help="sc_pt (default): the 64-replica simple-cubic line; the others measure the remaining "
                          "configurations (device throughput only)")
     args = ap.parse_args()

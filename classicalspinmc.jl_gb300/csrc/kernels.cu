@@ -73,7 +73,13 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
 // acceptance of dE - lambda' c -- since every proposal depends on lambda and V
 // as left by the one before.  Proposal q draws (site, u_acc) from Philox
 // counter (q, msweep, chain, CONS_A) and (u_phi, u_z) from (q, msweep, chain,
-// CONS_B); the site is floor(N x / 2^32) of the first word.
+// CONS_B); the site is floor(N x / 2^32) of the first word.  The uniforms
+// are 53-bit in double precision; a single-precision context takes 24-bit
+// uniforms (the top bits of the first word of each pair) and evaluates the
+// constraint, lambda' and the acceptance in single precision -- on this
+// device FP64 runs at a small fraction of the FP32 rate and the sequential
+// proposals would wait on it -- with V summed in FP64 at the start of the
+// sweep and lambda kept in FP64 between sweeps.
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainState cs, ConsArgs k, int kind,
                                                         uint32_t msweep, double T_override) {
@@ -99,12 +105,22 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
     const double T = T_override > 0 ? T_override : cs.T_slot[slot];
     const R sigma = (R)cs.sigma_slot[slot];
     const int pk = kind == CSMC_METROPOLIS_CONSTRAINT ? CSMC_METROPOLIS : CSMC_METROPOLIS_ADAPTIVE;
-    double lambda = k.lambda_slot[slot];
+    R lambda = (R)k.lambda_slot[slot];
+    R ux = (R)vx, uy = (R)vy, uz = (R)vz; // V in R from here on
+    const R invT = (R)(1.0 / T);
+    auto uniform = [](uint32_t a, uint32_t b) -> R {
+        if (sizeof(R) == 4) return (R)u24(a);
+        return (R)u53(a, b);
+    };
     unsigned long long acc = 0;
     const uint64_t n = (uint64_t)a.n_real;
+    // the draws of proposal q + 1 are computed while proposal q waits for its
+    // spins (they depend on nothing the proposal changes)
+    U4 A = philox4x32_10(0u, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
+    U4 B = philox4x32_10(0u, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
     for (uint64_t q = 0; q < n; q++) {
-        const U4 A = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
-        const U4 B = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+        const U4 An = philox4x32_10((uint32_t)(q + 1), msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
+        const U4 Bn = philox4x32_10((uint32_t)(q + 1), msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
         const int64_t i = (int64_t)(((uint64_t)A.x * n) >> 32);
         const int64_t d = a.ref2dev[i];
         const int b = a.tb.pat[d];
@@ -112,26 +128,26 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
         partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
         const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
         const V3<R> s = p.get(d);
-        const V3<R> sn = propose<R>(pk, a.S, sigma, s, (R)u53(B.x, B.y), (R)u53(B.z, B.w));
+        const V3<R> sn = propose<R>(pk, a.S, sigma, s, uniform(B.x, B.y), uniform(B.z, B.w));
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
-        const double w = k.w ? k.w[d] : 1.0;
-        const double nx = vx + w * ((double)sn.x - (double)s.x);
-        const double ny = vy + w * ((double)sn.y - (double)s.y);
-        const double nz = vz + w * ((double)sn.z - (double)s.z);
-        const double cv = constraint_value(k, nx, ny, nz);
-        const double nl = lambda - k.weight * cv;
-        const double x = (double)dE - nl * cv;
-        const bool accept = x < 0 ? true : u53(A.z, A.w) < exp(-x / T);
+        const R w = k.w ? (R)k.w[d] : R(1);
+        const R nx = ux + w * (sn.x - s.x), ny = uy + w * (sn.y - s.y), nz = uz + w * (sn.z - s.z);
+        const R cv = constraint_value<R>(k, nx, ny, nz);
+        const R nl = lambda - (R)k.weight * cv;
+        const R x = dE - nl * cv;
+        const bool accept = x < R(0) ? true : uniform(A.z, A.w) < Math<R>::exp_(boltz_arg(x, invT, T));
         if (accept) {
             p.set(d, sn);
-            vx = nx;
-            vy = ny;
-            vz = nz;
+            ux = nx;
+            uy = ny;
+            uz = nz;
             lambda = nl;
             acc++;
         }
+        A = An;
+        B = Bn;
     }
-    k.lambda_slot[slot] = lambda;
+    k.lambda_slot[slot] = (double)lambda;
     cs.sweep_acc[c] += acc;
 }
 

@@ -46,9 +46,10 @@ struct ConsArgs {
     double *lambda_slot; // mc.lambda of every slot
 };
 
-__host__ __device__ __forceinline__ double constraint_value(const ConsArgs &k, double vx, double vy, double vz) {
-    const double vv = vx * vx + vy * vy + vz * vz;
-    return k.g[0] * vx + k.g[1] * vy + k.g[2] * vz + k.q * vv + k.p * sqrt(vv) + k.c0;
+template <typename T>
+__host__ __device__ __forceinline__ T constraint_value(const ConsArgs &k, T vx, T vy, T vz) {
+    const T vv = vx * vx + vy * vy + vz * vz;
+    return (T)k.g[0] * vx + (T)k.g[1] * vy + (T)k.g[2] * vz + (T)k.q * vv + (T)k.p * sqrt(vv) + (T)k.c0;
 }
 
 // One lattice for the resident kernel (lives in device memory).
