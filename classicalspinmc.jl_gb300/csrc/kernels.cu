@@ -80,13 +80,12 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
 // device FP64 runs at a small fraction of the FP32 rate and the sequential
 // proposals would wait on it -- with V summed in FP64 at the start of the
 // sweep and lambda kept in FP64 between sweeps.
-template <typename R, bool CUB, bool QUA>
-__global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainState cs, ConsArgs k, int kind,
-                                                        uint32_t msweep, double T_override) {
-    const int r = blockIdx.x;
-    const int c = a.chain_base + r;
-    const Spins<R> p = replica(a, r);
-    double vx = 0.0, vy = 0.0, vz = 0.0;
+// V = sum_d w[d] s_d of a replica, summed by the calling warp in FP64 (every
+// lane gets it)
+template <typename R>
+__device__ __forceinline__ void constraint_v_sum(const SysArgs<R> &a, const Spins<R> &p, const ConsArgs &k, double &vx,
+                                                 double &vy, double &vz) {
+    vx = vy = vz = 0.0;
     for (int64_t d = threadIdx.x; d < a.tb.Np; d += 32) {
         const V3<R> s = p.get(d);
         const double w = k.w ? k.w[d] : 1.0;
@@ -100,6 +99,22 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
         vy += __shfl_xor_sync(0xffffffffu, vy, o);
         vz += __shfl_xor_sync(0xffffffffu, vz, o);
     }
+}
+// w_d (s' - s): the change of V when site d moves from s to s'
+template <typename R> __device__ __forceinline__ V3<R> constraint_step(const ConsArgs &k, int64_t d, V3<R> s, V3<R> sn) {
+    using F = Fp<R>;
+    const R w = k.w ? (R)k.w[d] : R(1);
+    return {F::mul(w, F::sub(sn.x, s.x)), F::mul(w, F::sub(sn.y, s.y)), F::mul(w, F::sub(sn.z, s.z))};
+}
+
+template <typename R, bool CUB, bool QUA>
+__global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainState cs, ConsArgs k, int kind,
+                                                        uint32_t msweep, double T_override) {
+    const int r = blockIdx.x;
+    const int c = a.chain_base + r;
+    const Spins<R> p = replica(a, r);
+    double vx, vy, vz;
+    constraint_v_sum(a, p, k, vx, vy, vz);
     if (threadIdx.x != 0) return;
     const int slot = cs.slot_of[c];
     const double T = T_override > 0 ? T_override : cs.T_slot[slot];
@@ -130,11 +145,11 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
         const V3<R> s = p.get(d);
         const V3<R> sn = propose<R>(pk, a.S, sigma, s, uniform(B.x, B.y), uniform(B.z, B.w));
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
-        const R w = k.w ? (R)k.w[d] : R(1);
-        const R nx = ux + w * (sn.x - s.x), ny = uy + w * (sn.y - s.y), nz = uz + w * (sn.z - s.z);
+        const V3<R> dv = constraint_step(k, d, s, sn);
+        const R nx = Fp<R>::add(ux, dv.x), ny = Fp<R>::add(uy, dv.y), nz = Fp<R>::add(uz, dv.z);
         const R cv = constraint_value<R>(k, nx, ny, nz);
-        const R nl = lambda - (R)k.weight * cv;
-        const R x = dE - nl * cv;
+        const R nl = Fp<R>::sub(lambda, Fp<R>::mul((R)k.weight, cv));
+        const R x = Fp<R>::sub(dE, Fp<R>::mul(nl, cv));
         const bool accept = x < R(0) ? true : uniform(A.z, A.w) < Math<R>::exp_(boltz_arg(x, invT, T));
         if (accept) {
             p.set(d, sn);
@@ -149,6 +164,109 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
     }
     k.lambda_slot[slot] = (double)lambda;
     cs.sweep_acc[c] += acc;
+}
+
+// The same sweep for lattices with bilinear terms only and at most CONS_NB
+// partners per site, 32 proposals at a time: lane j takes proposal q0 + j and
+// evaluates it against the state at the start of the batch (its draws, site,
+// proposed spin, dE, the change of V); the warp then decides the proposals
+// in order, in lockstep, exactly as the sequential kernel would (lambda and V
+// carried from one decision to the next), up to the first proposal whose
+// site or partners an accepted earlier proposal of the batch has changed;
+// that one and the rest are drawn again (same counters) in the next batch.
+// Every decision and every value equals the sequential kernel's.
+constexpr int CONS_NB = 15;
+template <typename R>
+__global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, ChainState cs, ConsArgs k, int kind,
+                                                              uint32_t msweep, double T_override) {
+    using F = Fp<R>;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int r = blockIdx.x, lane = threadIdx.x;
+    const int c = a.chain_base + r;
+    const Spins<R> p = replica(a, r);
+    double vx, vy, vz;
+    constraint_v_sum(a, p, k, vx, vy, vz);
+    const int slot = cs.slot_of[c];
+    const double T = T_override > 0 ? T_override : cs.T_slot[slot];
+    const R sigma = (R)cs.sigma_slot[slot];
+    const int pk = kind == CSMC_METROPOLIS_CONSTRAINT ? CSMC_METROPOLIS : CSMC_METROPOLIS_ADAPTIVE;
+    R lambda = (R)k.lambda_slot[slot];
+    R ux = (R)vx, uy = (R)vy, uz = (R)vz;
+    const R invT = (R)(1.0 / T);
+    auto uniform = [](uint32_t x, uint32_t y) -> R {
+        if (sizeof(R) == 4) return (R)u24(x);
+        return (R)u53(x, y);
+    };
+    const uint64_t n = (uint64_t)a.n_real;
+    const int64_t Np = a.tb.Np;
+    const int W2 = a.tb.W2;
+    unsigned long long acc = 0;
+    uint64_t q0 = 0;
+    while (q0 < n) {
+        const uint64_t q = q0 + (uint64_t)lane;
+        const bool live = q < n;
+        int64_t d = -1;
+        int64_t nb[CONS_NB];
+        V3<R> sn = {R(0), R(0), R(0)}, dv = {R(0), R(0), R(0)};
+        R dE = R(0), u = R(0);
+        if (live) {
+            const U4 A = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
+            const U4 B = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+            d = a.ref2dev[(int64_t)(((uint64_t)A.x * n) >> 32)];
+            const int b = a.tb.pat[d];
+#pragma unroll
+            for (int t = 0; t < CONS_NB; t++) nb[t] = t < W2 ? (int64_t)a.tb.p2[t * Np + d] : -1;
+            V3<R> hb, hc, hq;
+            partner_fields<R, uint32_t, false, false>(a.tb, a.cf, p, d, b, hb, hc, hq);
+            const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
+            const V3<R> s = p.get(d);
+            sn = propose<R>(pk, a.S, sigma, s, uniform(B.x, B.y), uniform(B.z, B.w));
+            dE = delta_e<R>(a.cf, b, s, sn, hext);
+            dv = constraint_step(k, d, s, sn);
+            u = uniform(A.z, A.w);
+        }
+        // the earlier lanes whose site is this lane's site or one of its partners
+        unsigned M = 0;
+        for (int j = 0; j < 32; j++) {
+            const int64_t dj = __shfl_sync(FULL, d, j);
+            bool hit = dj == d;
+#pragma unroll
+            for (int t = 0; t < CONS_NB; t++) hit = hit || nb[t] == dj;
+            if (j < lane && dj >= 0 && hit) M |= 1u << j;
+        }
+        // decisions in order (every lane computes the same)
+        const int nvalid = n - q0 < 32 ? (int)(n - q0) : 32;
+        unsigned taken = 0;
+        int stop = nvalid;
+        for (int j = 0; j < nvalid; j++) {
+            if (__shfl_sync(FULL, M, j) & taken) {
+                stop = j;
+                break;
+            }
+            const R ej = __shfl_sync(FULL, dE, j), uj = __shfl_sync(FULL, u, j);
+            const R nx = F::add(ux, __shfl_sync(FULL, dv.x, j)), ny = F::add(uy, __shfl_sync(FULL, dv.y, j)),
+                    nz = F::add(uz, __shfl_sync(FULL, dv.z, j));
+            const R cv = constraint_value<R>(k, nx, ny, nz);
+            const R nl = F::sub(lambda, F::mul((R)k.weight, cv));
+            const R x = F::sub(ej, F::mul(nl, cv));
+            const bool accept = x < R(0) ? true : uj < Math<R>::exp_(boltz_arg(x, invT, T));
+            if (accept) {
+                taken |= 1u << j;
+                ux = nx;
+                uy = ny;
+                uz = nz;
+                lambda = nl;
+            }
+        }
+        if (live && lane < stop && ((taken >> lane) & 1u)) p.set(d, sn);
+        acc += (unsigned long long)__popc(taken);
+        q0 += (uint64_t)stop;
+        __syncwarp();
+    }
+    if (lane == 0) {
+        k.lambda_slot[slot] = (double)lambda;
+        cs.sweep_acc[c] += acc;
+    }
 }
 
 // overrelaxation! body (monte_carlo.jl:128-137) on one colour class.
@@ -449,7 +567,10 @@ template <typename R>
 void launch_metro_constraint(const SysArgs<R> &a, const ChainState &cs, const ConsArgs &k, int kind, uint32_t msweep,
                              double T_override, cudaStream_t st) {
     if (a.n_rep <= 0 || a.n_real <= 0) return;
-    DISPATCH_CQ(a, k_metro_constraint, <<<a.n_rep, 32, 0, st>>>(a, cs, k, kind, msweep, T_override));
+    if (!a.cub && !a.qua && a.tb.W2 <= CONS_NB)
+        k_metro_constraint_batch<R><<<a.n_rep, 32, 0, st>>>(a, cs, k, kind, msweep, T_override);
+    else
+        DISPATCH_CQ(a, k_metro_constraint, <<<a.n_rep, 32, 0, st>>>(a, cs, k, kind, msweep, T_override));
 }
 
 void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,

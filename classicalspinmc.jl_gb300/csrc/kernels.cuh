@@ -46,10 +46,15 @@ struct ConsArgs {
     double *lambda_slot; // mc.lambda of every slot
 };
 
-template <typename T>
-__host__ __device__ __forceinline__ T constraint_value(const ConsArgs &k, T vx, T vy, T vz) {
-    const T vv = vx * vx + vy * vy + vz * vz;
-    return (T)k.g[0] * vx + (T)k.g[1] * vy + (T)k.g[2] * vz + (T)k.q * vv + (T)k.p * sqrt(vv) + (T)k.c0;
+// c(V) with explicit rounding (the sequential and the batched constrained
+// kernels evaluate it bit for bit alike)
+template <typename T> __device__ __forceinline__ T constraint_value(const ConsArgs &k, T vx, T vy, T vz) {
+    using F = Fp<T>;
+    const T vv = F::fma(vz, vz, F::fma(vy, vy, F::mul(vx, vx)));
+    T c = F::fma((T)k.g[2], vz, F::fma((T)k.g[1], vy, F::mul((T)k.g[0], vx)));
+    c = F::fma((T)k.q, vv, c);
+    c = F::fma((T)k.p, sqrt(vv), c);
+    return F::add(c, (T)k.c0);
 }
 
 // One lattice for the resident kernel (lives in device memory).
