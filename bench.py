@@ -275,7 +275,7 @@ def bench_ours(args, rank, world, dist):
                   "ms_per_step": 1e3 * t_e2e / e2e_steps,
                   "api": "csmc_set_spins_all + csmc_run + csmc_get_spins_all"}
 
-    # the plain FP64 one-replica-per-launch path on the same workload (spec comparison)
+    # the plain FP64 one-replica-per-launch path on the same workload (the metric compares against it)
     if rank == 0 and args.plain_steps > 0:
         ctx64 = m.monte_carlo.Context([lat], [R_REPL], precision="fp64", seed=SEED)
         ctx64.set_temperatures(temperatures())

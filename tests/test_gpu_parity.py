@@ -1,6 +1,6 @@
 """GPU kernels (through the C ABI) against the CPU oracle.
 
-Tolerances (from the spec parity gates):
+Tolerances (the parity gates of the path):
   local field / dE, FP64: |gpu - oracle| <= 1e-12 * sum|terms|
   local field / dE, FP32: |gpu - oracle| <= 1e-6  * sum|terms|
   colour-order overrelaxation / deterministic / Metropolis sweeps, FP64: 1e-12
