@@ -30,17 +30,21 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
     const int r = chain_lo + blockIdx.y;
     const int c = a.chain_base + r;
     const Spins<R> p = replica(a, r);
-    const int slot = cs.slot_of[c];
-    const double T = T_override > 0 ? T_override : cs.T_slot[slot];
-    // 1/T and sigma in R, formed once per block: FP64 division runs at a
-    // small fraction of the FP32 rate on this device
+    // T, 1/T and sigma formed once per block: FP64 arithmetic -- even one
+    // comparison per thread -- runs at a small fraction of the FP32 rate on
+    // this device
     __shared__ R s_invT, s_sigma;
+    __shared__ double s_T;
     if (threadIdx.x == 0) {
+        const int slot = cs.slot_of[c];
+        const double T = T_override > 0 ? T_override : cs.T_slot[slot];
+        s_T = T;
         s_invT = (R)(1.0 / T);
         s_sigma = (R)cs.sigma_slot[slot];
     }
     __syncthreads();
     const R invT = s_invT, sigma = s_sigma;
+    const double T = s_T; // used by the double-precision acceptance only
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
     unsigned acc = 0;
     if (i < count) {

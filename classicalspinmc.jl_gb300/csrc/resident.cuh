@@ -670,7 +670,8 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ double red[4];
     __shared__ int s_item;
     __shared__ int s_ok;
-    __shared__ double s_sigma;
+    __shared__ double s_sigma, s_T;
+    __shared__ R s_invT;
     __shared__ ResSys<R> s_sys;
     __shared__ R s_coef[K::kCoefSmem];
     __shared__ uint64_t pbar;
@@ -800,11 +801,16 @@ __global__ void __launch_bounds__(NT, 1)
                 if (q + 1 < w1) w1 = q + 1;
             }
             const int slot = __ldcg(cs.slot_of + c);
-            const double T = rd.T_override > 0 ? rd.T_override : __ldcg(cs.T_slot + slot);
-            if (threadIdx.x == 0)
+            // T and 1/T by thread 0 (FP64 division runs at a small fraction of
+            // the FP32 rate on this device)
+            if (threadIdx.x == 0) {
                 s_sigma = (rd.reset_sigma && w0 == rd.it0) ? rd.sigma0 : __ldcg(cs.sigma_slot + slot);
+                s_T = rd.T_override > 0 ? rd.T_override : __ldcg(cs.T_slot + slot);
+                s_invT = (R)(1.0 / s_T);
+            }
             __syncthreads();
-            const R invT = (R)(1.0 / T);
+            const double T = s_T;
+            const R invT = s_invT;
             double acc_total = 0.0;
 
             for (int64_t it = w0; it < w1; it++) {
