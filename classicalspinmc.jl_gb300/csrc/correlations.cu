@@ -31,7 +31,17 @@ template <> struct Vec4<double> {
     using T = double4;
 };
 
-__device__ __forceinline__ void sincos_(float t, float *s, float *c) { sincosf(t, s, c); }
+// Single precision: t reduced to [-pi, pi] by Cody-Waite reduction with 2 pi
+// split in two floats (W. J. Cody and W. Waite, Software Manual for the
+// Elementary Functions, 1980), then the hardware sine and cosine (absolute
+// error about 2^-21 on that interval).  t itself carries the rounding of the
+// single-precision dot product k.r, about 2^-24 |t|.
+__device__ __forceinline__ void sincos_(float t, float *s, float *c) {
+    const float n = rintf(t * 0.159154943091895336f);    // t / (2 pi), nearest integer
+    float r = __fmaf_rn(-n, 6.28318548202514648f, t);      // 2 pi rounded to float
+    r = __fmaf_rn(-n, -1.74845553146951305e-7f, r);        // 2 pi - that float
+    __sincosf(r, s, c);
+}
 __device__ __forceinline__ void sincos_(double t, double *s, double *c) { sincos(t, s, c); }
 } // namespace
 
