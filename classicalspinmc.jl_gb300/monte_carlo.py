@@ -11,20 +11,22 @@ The sweep plug point of the reference, ``alg(mc, T)``
 (``alg::FunctionWrapper{Float64,Tuple{MonteCarlo,Float64}}``, metropolis.jl:181-199),
 is kept: ``Metropolis()``, ``MetropolisAdaptive()`` and
 ``MetropolisFixedCone()`` return callables that run one device sweep and
-return the accepted count.  The constrained variants call an arbitrary host
-closure per proposal (metropolis.jl:36-58, :155-179) and are not provided.
+return the accepted count.  The constrained variants (metropolis.jl:36-58,
+:155-179) take a ``Constraint`` of closed form instead of a host closure.
+Output files (``outpath``) follow hdf5.jl's layout (``hdf5.py``).
 """
 from __future__ import annotations
 
 import copy
 import ctypes as C
 import math
+import os
 import warnings
 from dataclasses import dataclass
 
 import numpy as np
 
-from . import _lib
+from . import _lib, hdf5
 from .lattice import Lattice
 from .observables import Observables, mean_and_error, specific_heat, susceptibility
 
@@ -202,8 +204,11 @@ class MonteCarlo:
 
     Extra keywords of this implementation: ``precision`` ("fp64" or "fp32"),
     ``seed`` (Philox key), ``path`` ("auto", "resident", "global",
-    "per_replica").  Output files (``outpath``) are not written by this
-    package; pass ``outpath=""`` (the default).
+    "per_replica").  With ``outpath`` (a directory with its trailing
+    separator, as in the reference) the params file and one configuration
+    file per replica are created as monte_carlo.jl:95-116 does for its ranks
+    (replica r plays rank r): ``mc.outpath`` is the file of the one replica,
+    or the list of the replicas' files.
     """
 
     def __init__(self, T, lattice: Lattice, parameters: dict, *, constraint=None, weight: float = 0.0,
@@ -215,8 +220,6 @@ class MonteCarlo:
         if constraint is not None and not isinstance(constraint, Constraint):
             raise TypeError("constraint must be a Constraint: the device evaluates c = g.V + q|V|^2 + p|V| + c0 "
                             "of V = sum_i w_i s_i, not an arbitrary function")
-        if outpath:
-            warnings.warn("outpath given: HDF5 output is not written by this package")
         self.temperatures = np.atleast_1d(np.asarray(T, dtype=np.float64)).copy()
         self.lattice = copy.deepcopy(lattice)  # monte_carlo.jl:74
         self.parameters = MCParamsBuffer(dict(parameters))
@@ -239,6 +242,21 @@ class MonteCarlo:
         self.accepted = np.zeros(R)
         self.exchanged = np.zeros(R)
         self.initial_configurations = {}  # parallel_tempering(saveIC=...): {rank: {timestep: spins}}
+        self.outpaths = []
+        if outpath:  # monte_carlo.jl:95-113
+            self.outpaths = [f"{outpath}{outprefix}_{r}.h5" for r in range(R)]
+            if not os.path.isdir(outpath):
+                os.mkdir(outpath)
+            paramsfile = f"{outpath}{outprefix}.h5.params"
+            if not os.path.isfile(paramsfile) and overwrite:
+                hdf5.create_params_file(self, paramsfile)
+                if inparams:
+                    hdf5.write_attributes(paramsfile, dict(inparams))
+            for r, fn in enumerate(self.outpaths):
+                if not os.path.isfile(fn) and overwrite:
+                    print(f"Creating new file {os.path.basename(fn)} for output on rank {r}")
+                    hdf5.initialize_hdf5(self, paramsfile, r)
+            self.outpath = self.outpaths[0] if R == 1 else list(self.outpaths)
 
     # -- state --------------------------------------------------------------
     @property
@@ -399,10 +417,17 @@ def simulated_annealing(mc: MonteCarlo, schedule, T0: float = 1.0, alg: _Alg | N
     p = mc.parameters
     R = mc.n_replicas
     acc = np.zeros((len(temps), R))
-    if temps:
-        t = np.asarray(temps, dtype=np.float64)
-        mc.ctx.call("csmc_anneal", _lib.ptr(t, C.c_double), len(temps), p.t_thermalization,
-                    p.overrelaxation_rate, alg.kind, C.c_double(mc.sigma0), _PATHS[mc.path], _lib.ptr(acc, C.c_double))
+    t = np.asarray(temps, dtype=np.float64)
+    # with output files, one call per temperature and the checkpoint after it
+    # (monte_carlo.jl:186-188); the random streams are keyed by the sweep
+    # counters the context carries, so the chains do not depend on the split
+    steps = [(k, k + 1) for k in range(len(temps))] if mc.outpaths else ([(0, len(temps))] if temps else [])
+    for a, b in steps:
+        mc.ctx.call("csmc_anneal", _lib.ptr(t[a:], C.c_double), b - a, p.t_thermalization,
+                    p.overrelaxation_rate, alg.kind, C.c_double(mc.sigma0), _PATHS[mc.path],
+                    _lib.ptr(acc[a:], C.c_double))
+        if mc.outpaths:
+            hdf5.write_MC_checkpoint(mc)
     if verbose:
         total = p.t_thermalization * mc.lattice.size / (p.overrelaxation_rate or 1)
         for T, a in zip(temps, acc[:, 0]):
@@ -431,9 +456,12 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     Like the reference, report_interval and checkpoint_rate must be nonzero
     (``sweep % 0`` throws a DivideError at monte_carlo.jl:355 and :383).
     ``saveIC`` lists ranks (slots) whose configuration is saved at every
-    checkpoint of the measurement phase (monte_carlo.jl:353-364); the
-    configurations are kept in ``mc.initial_configurations[rank][timestep]``
-    (3 x N arrays) instead of ``IC_<rank>/IC_<timestep>.h5`` files.
+    checkpoint of the measurement phase (monte_carlo.jl:353-364): kept in
+    ``mc.initial_configurations[rank][timestep]`` (3 x N arrays) and, with
+    output files, written to ``IC_<rank>/IC_<timestep>.h5`` beside them.
+    With output files every replica's file also gets the spins at those
+    checkpoints (write_MC_checkpoint) and the observables at the end
+    (write_final_observables, monte_carlo.jl:387-391).
     Returns the per-replica energy and |M| series and the derived observables.
     """
     alg = Metropolis() if alg is None else alg
@@ -459,8 +487,16 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
     def is_corr(it):  # correlations at the probe, after the exchange (monte_carlo.jl:371-375)
         return mc.corr and p.probe_rate > 0 and it >= p.t_thermalization and it % p.probe_rate == 0
 
-    def is_ic(it):  # initial configurations at the checkpoints of the measurement (monte_carlo.jl:353-364)
-        return bool(save) and it >= p.t_thermalization and it % p.checkpoint_rate == 0
+    out = bool(mc.outpaths)
+
+    def is_ic(it):  # checkpoints of the measurement phase (monte_carlo.jl:353-364)
+        return (out or bool(save)) and it >= p.t_thermalization and it % p.checkpoint_rate == 0
+
+    if out and save:
+        for r in save:
+            d = os.path.join(os.path.dirname(mc.outpaths[r]), f"IC_{r}")
+            if not os.path.isdir(d):
+                os.mkdir(d)
 
     def pieces(a, b):
         """[a, b) split after every iteration whose end state is read on the host."""
@@ -485,10 +521,17 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
                 ssf = structure_factors(mc, mc.momentum_vectors)
                 for r in range(R):
                     mc.observables[r].push_correlations(ssf[r])
-            if is_ic(b - 1):  # write_initial_configuration of IC_<rank>/IC_<timestep>, kept in memory
+            if is_ic(b - 1):
                 timestep = (b - 1 - p.t_thermalization) // p.checkpoint_rate
+                spins = [mc.spins(r) for r in range(R)] if out else {r: mc.spins(r) for r in save}
+                if out:
+                    hdf5.write_MC_checkpoint(mc, spins)
                 for r in save:
-                    mc.initial_configurations.setdefault(r, {})[timestep] = mc.spins(r)
+                    mc.initial_configurations.setdefault(r, {})[timestep] = spins[r]
+                    if out:
+                        hdf5.write_initial_configuration(
+                            os.path.join(os.path.dirname(mc.outpaths[r]), f"IC_{r}", f"IC_{timestep}.h5"),
+                            mc, r, spins[r])
         mc.accepted += acc
         mc.exchanged += exc
         start += n
@@ -500,6 +543,8 @@ def parallel_tempering(mc: MonteCarlo, saveIC=(), alg: _Alg | None = None, verbo
         for e, m in zip(E[:, r], M[:, r]):
             mc.observables[r].push(e, m)
     mc.sync()
+    if out:
+        hdf5.write_final_observables(mc, verbose)
     return {"energy": E, "magnetization": M, "summary": summarize(mc, E, M)}
 
 
@@ -574,7 +619,9 @@ def _print_runtime_statistics(mc, t, acc, exc, n):
 
 
 def summarize(mc: MonteCarlo, E: np.ndarray, M: np.ndarray) -> list[dict]:
-    """write_final_observables content (hdf5.jl:204-239) per replica, without the file."""
+    """The derived observables of write_final_observables (hdf5.jl:204-239) per
+    replica, with absolute errors throughout (the files hold the reference's
+    relative errors for the specific heat and the susceptibility)."""
     out = []
     N = mc.lattice.size
     for r in range(mc.n_replicas):
