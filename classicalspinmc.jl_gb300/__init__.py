@@ -18,5 +18,9 @@ from .monte_carlo import (MCParamsBuffer, Metropolis, MetropolisAdaptive, Metrop
                           compute_equal_time_correlations, structure_factors)
 from . import examples  # noqa: F401
 from .observables import specific_heat, susceptibility  # noqa: F401
+from .hdf5 import (create_params_file, h5open, overwrite_keys, read_lattice, read_spin_configuration,  # noqa: F401
+                   write_MC_checkpoint)
+from .reciprocal import get_allowed_wavevectors, get_k_path, get_k_plane, reciprocal  # noqa: F401
+from .spin_correlations import compute_equal_time_structure_factor, runEqualTimeStructureFactor  # noqa: F401
 from .unit_cell import (FCC, BreathingPyrochlore, Honeycomb, Pyrochlore, Square, Triangular,  # noqa: F401
                         UnitCell, addBasisSite, addBilinear, addCubic, addOnSite, addQuartic, addZeemanCoupling)

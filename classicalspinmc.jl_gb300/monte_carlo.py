@@ -353,7 +353,11 @@ def structure_factors(x, ks) -> np.ndarray:
     slot at once: ks is dim x N_k (the reference's layout); returns an array
     [slot, 9, N_k] of Re(S_a(k) conj(S_b(k))) / N, row 3a+b."""
     ctx, mc = _context_of(x)
-    lat = mc.lattice if mc is not None else x
+    return context_structure_factors(ctx, mc.lattice if mc is not None else x, ks)
+
+
+def context_structure_factors(ctx: Context, lat: Lattice, ks) -> np.ndarray:
+    """structure_factors of every slot of a context of one lattice."""
     ks = np.asfortranarray(np.atleast_2d(np.asarray(ks, dtype=np.float64)))
     pos = np.asfortranarray(lat.site_positions, dtype=np.float64)
     dim, n_k = ks.shape
