@@ -229,38 +229,39 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
             dv = constraint_step(k, d, s, sn);
             u = uniform(A.z, A.w);
         }
-        // the earlier lanes whose site is this lane's site or one of its partners
-        unsigned M = 0;
-        for (int j = 0; j < 32; j++) {
+        // Decisions in order, one accepted proposal per round: every lane of
+        // [start, stop) decides against the current state (V, lambda), which
+        // is the state the sequential order gives it up to the first lane
+        // that accepts; that lane's V and lambda become the state, the lanes
+        // after it decide again in the next round, and the first later lane
+        // that shares a site with it bounds the batch.  The arithmetic of
+        // every decision is the sequential kernel's.
+        const int nvalid = n - q0 < 32 ? (int)(n - q0) : 32;
+        unsigned taken = 0;
+        int stop = nvalid, start = 0;
+        while (start < stop) {
+            const R nx = F::add(ux, dv.x), ny = F::add(uy, dv.y), nz = F::add(uz, dv.z);
+            const R cv = constraint_value<R>(k, nx, ny, nz);
+            const R nl = F::sub(lambda, F::mul((R)k.weight, cv));
+            const R x = F::sub(dE, F::mul(nl, cv));
+            const bool in = lane >= start && lane < stop;
+            const bool accept = in && (x < R(0) ? true : u < Math<R>::exp_(boltz_arg(x, invT, T)));
+            const unsigned ball = __ballot_sync(FULL, accept);
+            if (ball == 0u) break;
+            const int j = __ffs((int)ball) - 1;
+            taken |= 1u << j;
+            ux = __shfl_sync(FULL, nx, j);
+            uy = __shfl_sync(FULL, ny, j);
+            uz = __shfl_sync(FULL, nz, j);
+            lambda = __shfl_sync(FULL, nl, j);
+            // the later lanes whose site is the accepted site or a partner of theirs
             const int64_t dj = __shfl_sync(FULL, d, j);
             bool hit = dj == d;
 #pragma unroll
             for (int t = 0; t < CONS_NB; t++) hit = hit || nb[t] == dj;
-            if (j < lane && dj >= 0 && hit) M |= 1u << j;
-        }
-        // decisions in order (every lane computes the same)
-        const int nvalid = n - q0 < 32 ? (int)(n - q0) : 32;
-        unsigned taken = 0;
-        int stop = nvalid;
-        for (int j = 0; j < nvalid; j++) {
-            if (__shfl_sync(FULL, M, j) & taken) {
-                stop = j;
-                break;
-            }
-            const R ej = __shfl_sync(FULL, dE, j), uj = __shfl_sync(FULL, u, j);
-            const R nx = F::add(ux, __shfl_sync(FULL, dv.x, j)), ny = F::add(uy, __shfl_sync(FULL, dv.y, j)),
-                    nz = F::add(uz, __shfl_sync(FULL, dv.z, j));
-            const R cv = constraint_value<R>(k, nx, ny, nz);
-            const R nl = F::sub(lambda, F::mul((R)k.weight, cv));
-            const R x = F::sub(ej, F::mul(nl, cv));
-            const bool accept = x < R(0) ? true : uj < Math<R>::exp_(boltz_arg(x, invT, T));
-            if (accept) {
-                taken |= 1u << j;
-                ux = nx;
-                uy = ny;
-                uz = nz;
-                lambda = nl;
-            }
+            const unsigned conf = __ballot_sync(FULL, lane > j && lane < stop && hit);
+            if (conf != 0u) stop = __ffs((int)conf) - 1;
+            start = j + 1;
         }
         if (live && lane < stop && ((taken >> lane) & 1u)) p.set(d, sn);
         acc += (unsigned long long)__popc(taken);
