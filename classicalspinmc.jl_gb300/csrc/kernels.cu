@@ -206,20 +206,44 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
     const int W2 = a.tb.W2;
     unsigned long long acc = 0;
     uint64_t q0 = 0;
+    // What does not depend on the spins -- the draws, the site, its pattern
+    // and partner indices -- is fetched for the next batch of 32 while the
+    // warp decides the current one; it is used when the current batch is
+    // not cut short (else fetched again).
+    uint64_t pf_q0 = UINT64_MAX;
+    U4 pA = {0u, 0u, 0u, 0u}, pB = {0u, 0u, 0u, 0u};
+    int64_t pd = -1, pnb[CONS_NB];
+    int pbs = 0;
+    auto fetch = [&](uint64_t qq, U4 &A, U4 &B, int64_t &dd, int &bb, int64_t *nn) {
+        A = philox4x32_10((uint32_t)qq, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
+        B = philox4x32_10((uint32_t)qq, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+        dd = a.ref2dev[(int64_t)(((uint64_t)A.x * n) >> 32)];
+        bb = a.tb.pat[dd];
+#pragma unroll
+        for (int t = 0; t < CONS_NB; t++) nn[t] = t < W2 ? (int64_t)a.tb.p2[t * Np + dd] : -1;
+    };
     while (q0 < n) {
         const uint64_t q = q0 + (uint64_t)lane;
         const bool live = q < n;
         int64_t d = -1;
         int64_t nb[CONS_NB];
+#pragma unroll
+        for (int t = 0; t < CONS_NB; t++) nb[t] = -1;
         V3<R> sn = {R(0), R(0), R(0)}, dv = {R(0), R(0), R(0)};
         R dE = R(0), u = R(0);
         if (live) {
-            const U4 A = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
-            const U4 B = philox4x32_10((uint32_t)q, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
-            d = a.ref2dev[(int64_t)(((uint64_t)A.x * n) >> 32)];
-            const int b = a.tb.pat[d];
+            U4 A, B;
+            int b;
+            if (pf_q0 == q0) {
+                A = pA;
+                B = pB;
+                d = pd;
+                b = pbs;
 #pragma unroll
-            for (int t = 0; t < CONS_NB; t++) nb[t] = t < W2 ? (int64_t)a.tb.p2[t * Np + d] : -1;
+                for (int t = 0; t < CONS_NB; t++) nb[t] = pnb[t];
+            } else {
+                fetch(q, A, B, d, b, nb);
+            }
             V3<R> hb, hc, hq;
             partner_fields<R, uint32_t, false, false>(a.tb, a.cf, p, d, b, hb, hc, hq);
             const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
@@ -229,6 +253,8 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
             dv = constraint_step(k, d, s, sn);
             u = uniform(A.z, A.w);
         }
+        pf_q0 = q0 + 32;
+        if (pf_q0 + (uint64_t)lane < n) fetch(pf_q0 + (uint64_t)lane, pA, pB, pd, pbs, pnb);
         // Decisions in order, one accepted proposal per round: every lane of
         // [start, stop) decides against the current state (V, lambda), which
         // is the state the sequential order gives it up to the first lane
