@@ -50,10 +50,16 @@ struct ConsArgs {
 // kernels evaluate it bit for bit alike)
 template <typename T> __device__ __forceinline__ T constraint_value(const ConsArgs &k, T vx, T vy, T vz) {
     using F = Fp<T>;
-    const T vv = F::fma(vz, vz, F::fma(vy, vy, F::mul(vx, vx)));
     T c = F::fma((T)k.g[2], vz, F::fma((T)k.g[1], vy, F::mul((T)k.g[0], vx)));
-    c = F::fma((T)k.q, vv, c);
-    c = F::fma((T)k.p, sqrt(vv), c);
+    // a zero q or p adds nothing (fma(0, x, c) = c for finite x, up to the
+    // sign of a zero c, which the + c0 below makes +0 either way); skipping
+    // them takes |V|^2 and the square root off the chain of the sequential
+    // decisions
+    if (k.q != 0.0 || k.p != 0.0) {
+        const T vv = F::fma(vz, vz, F::fma(vy, vy, F::mul(vx, vx)));
+        c = F::fma((T)k.q, vv, c);
+        c = F::fma((T)k.p, sqrt(vv), c);
+    }
     return F::add(c, (T)k.c0);
 }
 
