@@ -24,9 +24,16 @@ template <typename R> __device__ __forceinline__ Spins<R> replica(const SysArgs<
 
 // One Metropolis colour step: every site of the class proposes once
 // (metropolis.jl:65-82, with site order given by the colouring).
+// The colour-sweep kernels are launched as programmatic dependents of the
+// kernel before them (launch_dep): the launch overlaps the end of that kernel,
+// and this wait -- a no-op for an ordinary launch -- holds every thread until
+// that kernel has completed and its writes are visible.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs, int64_t start, int64_t count,
                                                      int chain_lo, int kind, uint32_t msweep, double T_override) {
+    pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const int c = a.chain_base + r;
     const Spins<R> p = replica(a, r);
@@ -303,6 +310,7 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
 // overrelaxation! body (monte_carlo.jl:128-137) on one colour class.
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+    pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
@@ -317,6 +325,7 @@ __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, i
 // deterministic_updates! body (monte_carlo.jl:205-210) on one colour class.
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+    pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
     const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
@@ -544,28 +553,49 @@ template <typename R> static dim3 grid_for(int64_t n, int chains) {
         else KERNEL<R, false, false> __VA_ARGS__;                                                                      \
     } while (0)
 
+// A launch with programmatic stream serialization (see pdl_wait).
+template <typename... KArgs, typename... Args>
+static void launch_dep(void (*kern)(KArgs...), dim3 g, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = dim3(GB);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...) != cudaSuccess) {
+        (void)cudaGetLastError();
+        kern<<<g, GB, 0, st>>>(static_cast<KArgs>(args)...); // an ordinary launch reports its own error
+    }
+}
+
+#define PICK_CQ(a, KERNEL)                                                                                             \
+    ((a).cub && (a).qua ? KERNEL<R, true, true>                                                                       \
+                        : (a).cub ? KERNEL<R, true, false> : (a).qua ? KERNEL<R, false, true> : KERNEL<R, false, false>)
+
 template <typename R>
 void launch_metro_colour(const SysArgs<R> &a, const ChainState &cs, int64_t start, int64_t count, int chain_lo,
                          int n_chains, int kind, uint32_t msweep, double T_override, cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    dim3 g = grid_for<R>(count, n_chains);
-    DISPATCH_CQ(a, k_metro_colour, <<<g, GB, 0, st>>>(a, cs, start, count, chain_lo, kind, msweep, T_override));
+    launch_dep(PICK_CQ(a, k_metro_colour), grid_for<R>(count, n_chains), st, a, cs, start, count, chain_lo, kind,
+               msweep, T_override);
 }
 
 template <typename R>
 void launch_or_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
                       cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    dim3 g = grid_for<R>(count, n_chains);
-    DISPATCH_CQ(a, k_or_colour, <<<g, GB, 0, st>>>(a, start, count, chain_lo));
+    launch_dep(PICK_CQ(a, k_or_colour), grid_for<R>(count, n_chains), st, a, start, count, chain_lo);
 }
 
 template <typename R>
 void launch_det_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
                        cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    dim3 g = grid_for<R>(count, n_chains);
-    DISPATCH_CQ(a, k_det_colour, <<<g, GB, 0, st>>>(a, start, count, chain_lo));
+    launch_dep(PICK_CQ(a, k_det_colour), grid_for<R>(count, n_chains), st, a, start, count, chain_lo);
 }
 
 int64_t partial_blocks(int64_t Np) { return (Np + RB - 1) / RB; }
