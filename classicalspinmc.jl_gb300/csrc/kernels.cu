@@ -346,6 +346,7 @@ constexpr int RK = 8, RB = GB * RK;
 // Per-block partial sums of total_energy (hamiltonian.jl:70-132).
 template <typename R, bool CUB, bool QUA>
 __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, double *part) {
+    pdl_wait();
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
@@ -362,6 +363,7 @@ __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, 
 
 // Per-block partial sums of sum_i s_i (observables.jl:12-18).
 template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArgs<R> a, int chain_lo, double *part) {
+    pdl_wait();
     __shared__ double scratch[GB / 32];
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
@@ -389,6 +391,7 @@ template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArg
 // width = values per block entry (1: energy, 3: magnetisation -> norm).
 __global__ void k_reduce_rows(const double *part, int64_t nblk, int width, double *out_chain, int chain_base,
                               int chain_lo) {
+    pdl_wait();
     __shared__ double scratch[GB / 32];
     const int row = blockIdx.x;
     double v[3] = {0, 0, 0};
@@ -408,6 +411,7 @@ __global__ void k_reduce_rows(const double *part, int64_t nblk, int width, doubl
 // metropolis_constraint_adaptive! (:175-177).
 __global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, double n_sites, double sigma0,
                               double *last_acc) {
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int c = chain_first + k;
@@ -437,6 +441,7 @@ __global__ void k_after_metro(ChainState cs, int chain_first, int n, int kind, d
 // and |M| of the replica that now sits in it.  kq < 0: no record.
 __global__ void k_exchange(ChainState cs, const int2 *lattices, int64_t it, int swap_rate, uint32_t k0, uint32_t k1,
                            int do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots) {
+    pdl_wait();
     const int sys = blockIdx.x;
     const int slot_base = lattices[sys].x, n_rep = lattices[sys].y;
     if (do_swap) exchange_slots(cs, sys, slot_base, n_rep, it, swap_rate, k0, k1);
@@ -555,10 +560,10 @@ template <typename R> static dim3 grid_for(int64_t n, int chains) {
 
 // A launch with programmatic stream serialization (see pdl_wait).
 template <typename... KArgs, typename... Args>
-static void launch_dep(void (*kern)(KArgs...), dim3 g, cudaStream_t st, Args... args) {
+static void launch_dep_b(void (*kern)(KArgs...), dim3 g, int block, cudaStream_t st, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = g;
-    cfg.blockDim = dim3(GB);
+    cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
@@ -568,8 +573,13 @@ static void launch_dep(void (*kern)(KArgs...), dim3 g, cudaStream_t st, Args... 
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...) != cudaSuccess) {
         (void)cudaGetLastError();
-        kern<<<g, GB, 0, st>>>(static_cast<KArgs>(args)...); // an ordinary launch reports its own error
+        kern<<<g, block, 0, st>>>(static_cast<KArgs>(args)...); // an ordinary launch reports its own error
     }
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_dep(void (*kern)(KArgs...), dim3 g, cudaStream_t st, Args... args) {
+    launch_dep_b(kern, g, GB, st, args...);
 }
 
 #define PICK_CQ(a, KERNEL)                                                                                             \
@@ -605,8 +615,9 @@ void launch_energy(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int 
                    cudaStream_t st) {
     if (n_chains <= 0) return;
     const dim3 g((unsigned)partial_blocks(a.tb.Np), (unsigned)n_chains);
-    DISPATCH_CQ(a, k_energy_part, <<<g, GB, 0, st>>>(a, chain_lo, part));
-    k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 1, cs.E_chain, a.chain_base, chain_lo);
+    launch_dep(PICK_CQ(a, k_energy_part), g, st, a, chain_lo, part);
+    launch_dep(k_reduce_rows, dim3(n_chains), st, (const double *)part, (int64_t)g.x, 1, cs.E_chain, a.chain_base,
+               chain_lo);
 }
 
 template <typename R>
@@ -614,14 +625,16 @@ void launch_magnet(const SysArgs<R> &a, const ChainState &cs, int chain_lo, int 
                    cudaStream_t st) {
     if (n_chains <= 0) return;
     const dim3 g((unsigned)partial_blocks(a.tb.Np), (unsigned)n_chains);
-    k_magnet_part<R><<<g, GB, 0, st>>>(a, chain_lo, part);
-    k_reduce_rows<<<n_chains, GB, 0, st>>>(part, g.x, 3, cs.M_chain, a.chain_base, chain_lo);
+    launch_dep(k_magnet_part<R>, g, st, a, chain_lo, part);
+    launch_dep(k_reduce_rows, dim3(n_chains), st, (const double *)part, (int64_t)g.x, 3, cs.M_chain, a.chain_base,
+               chain_lo);
 }
 
 void launch_after_metro(const ChainState &cs, int chain_first, int n, int kind, int64_t n_sites, double sigma0,
                         double *last_acc, cudaStream_t st) {
     if (n <= 0) return;
-    k_after_metro<<<(n + 127) / 128, 128, 0, st>>>(cs, chain_first, n, kind, (double)n_sites, sigma0, last_acc);
+    launch_dep_b(k_after_metro, dim3((n + 127) / 128), 128, st, cs, chain_first, n, kind, (double)n_sites, sigma0,
+                 last_acc);
 }
 
 template <typename R>
@@ -636,8 +649,8 @@ void launch_metro_constraint(const SysArgs<R> &a, const ChainState &cs, const Co
 
 void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices, int64_t it, int swap_rate, uint32_t k0,
                      uint32_t k1, bool do_swap, double *rec_E, double *rec_M, int64_t kq, int n_slots, cudaStream_t st) {
-    k_exchange<<<n_lattices, 256, 0, st>>>(cs, lattices, it, swap_rate, k0, k1, do_swap ? 1 : 0, rec_E, rec_M, kq,
-                                           n_slots);
+    launch_dep_b(k_exchange, dim3(n_lattices), 256, st, cs, lattices, it, swap_rate, k0, k1, do_swap ? 1 : 0, rec_E,
+                 rec_M, kq, n_slots);
 }
 
 template <typename R>
