@@ -55,8 +55,10 @@ __global__ void __launch_bounds__(SF_THREADS)
                        int chain_base, int slot_base, double *__restrict__ out) {
     using V4 = typename Vec4<R>::T;
     constexpr int SF_CH = sf_chunk<R>();
-    __shared__ R s_cos[SF_KT][SF_CH];
-    __shared__ R s_sin[SF_KT][SF_CH];
+    // phases stored [site][wavevector]: a thread's SF_KK wavevectors of one
+    // site are one vector load
+    __shared__ __align__(16) R s_cos[SF_CH][SF_KT];
+    __shared__ __align__(16) R s_sin[SF_CH][SF_KT];
     __shared__ V4 s_spin[SF_CH][SF_RG];
     const int rl = threadIdx.x % SF_RG, kg = threadIdx.x / SF_RG;
     const int64_t k0 = (int64_t)blockIdx.x * SF_KT;
@@ -70,7 +72,7 @@ __global__ void __launch_bounds__(SF_THREADS)
     for (int64_t c0 = 0; c0 < Np; c0 += SF_CH) {
         __syncthreads(); // the previous chunk is consumed
         for (int e = threadIdx.x; e < SF_KT * SF_CH; e += SF_THREADS) {
-            const int kk = e / SF_CH, ii = e - kk * SF_CH;
+            const int ii = e / SF_KT, kk = e - ii * SF_KT;
             const int64_t k = k0 + kk, i = c0 + ii;
             R c = R(0), s = R(0);
             if (k < n_k && i < Np) {
@@ -79,8 +81,8 @@ __global__ void __launch_bounds__(SF_THREADS)
                                        Fp<R>::fma(ks[3 * k + 1], pos[3 * i + 1], Fp<R>::mul(ks[3 * k], pos[3 * i])));
                 sincos_(t, &s, &c);
             }
-            s_cos[kk][ii] = c;
-            s_sin[kk][ii] = -s;
+            s_cos[ii][kk] = c;
+            s_sin[ii][kk] = -s;
         }
         for (int e = threadIdx.x; e < SF_CH * SF_RG; e += SF_THREADS) {
             const int ii = e / SF_RG, rr = e - ii * SF_RG;
@@ -100,9 +102,22 @@ __global__ void __launch_bounds__(SF_THREADS)
 #pragma unroll 4
         for (int ii = 0; ii < SF_CH; ii++) {
             const V4 v = s_spin[ii][rl];
+            R cq[SF_KK], sq[SF_KK];
+            if constexpr (sizeof(R) == 4 && SF_KK % 4 == 0) {
+#pragma unroll
+                for (int q = 0; q < SF_KK; q += 4) {
+                    const float4 c4 = *reinterpret_cast<const float4 *>(&s_cos[ii][kg * SF_KK + q]);
+                    const float4 s4 = *reinterpret_cast<const float4 *>(&s_sin[ii][kg * SF_KK + q]);
+                    cq[q] = c4.x, cq[q + 1] = c4.y, cq[q + 2] = c4.z, cq[q + 3] = c4.w;
+                    sq[q] = s4.x, sq[q + 1] = s4.y, sq[q + 2] = s4.z, sq[q + 3] = s4.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < SF_KK; q++) cq[q] = s_cos[ii][kg * SF_KK + q], sq[q] = s_sin[ii][kg * SF_KK + q];
+            }
 #pragma unroll
             for (int q = 0; q < SF_KK; q++) {
-                const R c = s_cos[kg * SF_KK + q][ii], s = s_sin[kg * SF_KK + q][ii];
+                const R c = cq[q], s = sq[q];
                 re[q][0] = Fp<R>::fma(c, v.x, re[q][0]);
                 re[q][1] = Fp<R>::fma(c, v.y, re[q][1]);
                 re[q][2] = Fp<R>::fma(c, v.z, re[q][2]);
