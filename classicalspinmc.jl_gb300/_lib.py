@@ -25,6 +25,7 @@ i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
 f64p = C.POINTER(C.c_double)
 u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
 
 
 class CSMCError(RuntimeError):
@@ -109,6 +110,7 @@ SIGNATURES = {
     "csmc_total_energy": (C.c_int, [_vp, f64p]),
     "csmc_magnetization": (C.c_int, [_vp, f64p]),
     "csmc_metropolis_sweep": (C.c_int, [_vp, C.c_int32, f64p]),
+    "csmc_metropolis_sweep_at": (C.c_int, [_vp, C.c_int32, f64p, C.c_int32, f64p]),
     "csmc_overrelax_sweep": (C.c_int, [_vp]),
     "csmc_deterministic_sweeps": (C.c_int, [_vp, C.c_int64]),
     "csmc_replay": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_double, f64p, C.c_int64, i64p, f64p, f64p, f64p,
@@ -125,6 +127,8 @@ SIGNATURES = {
     "csmc_persistent": (C.c_int, [_vp, i32p]),
     "csmc_set_renormalize": (C.c_int, [_vp, C.c_int32]),
     "csmc_spin_length_drift": (C.c_int, [_vp, f64p]),
+    "csmc_debug_philox": (C.c_int, [u32p, u32p, C.c_int64, u32p]),
+    "csmc_debug_device_allocs": (C.c_int, [i64p]),
     "csmc_last_run_stats": (C.c_int, [_vp, f64p, i64p, f64p, i64p]),
 }
 

@@ -3,6 +3,7 @@
 // kernels.cu in the cadence of simulated_annealing! / parallel_tempering!
 // (monte_carlo.jl:157-190, :288-388).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -35,6 +36,10 @@ static void require(bool ok, int code, const std::string &msg) {
     if (!ok) throw Error(code, msg);
 }
 
+// Device allocations made by the library since the process started
+// (csmc_debug_device_allocs).
+static std::atomic<int64_t> g_device_allocs{0};
+
 template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
@@ -48,7 +53,10 @@ template <typename T> struct DevBuf {
         if (p) cudaFree(p);
         p = nullptr;
         n = count;
-        if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+        if (count) {
+            g_device_allocs++;
+            CK(cudaMalloc(&p, count * sizeof(T)));
+        }
     }
     void upload(const T *src, size_t count) {
         alloc(count);
@@ -109,6 +117,7 @@ struct Ctx {
     cudaStream_t st = nullptr;
     DevBuf<int32_t> slot_of, chain_of;
     DevBuf<double> T_slot, sigma_slot, acc_slot, exch_slot, E_chain, M_chain, last_acc;
+    DevBuf<double> T_stash; // mc.T of every slot during a csmc_metropolis_sweep_at call
     DevBuf<unsigned long long> sweep_acc;
     DevBuf<unsigned int> drift_bits;
     DevBuf<int> error_flag, work_ctr;
@@ -561,6 +570,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     C->chain_of.upload(ident);
     std::vector<double> ones(nc, 1.0), sig(nc, 60.0), zeros(nc, 0.0);
     C->T_slot.upload(ones);
+    C->T_stash.upload(ones);
     C->sigma_slot.upload(sig);
     C->acc_slot.upload(zeros);
     C->exch_slot.upload(zeros);
@@ -1255,7 +1265,31 @@ static void ensure_exact(Ctx &C, System &S) {
 
 using namespace csmc;
 
-#define API_BEGIN try {
+// The device of the context an entry point works on is made current for the
+// call and the caller's device restored on return: a context keeps working
+// when its caller has switched devices in between.  ctx_of() pins it.
+struct DeviceScope {
+    static thread_local DeviceScope *cur;
+    DeviceScope *outer;
+    int prev = -1;
+    DeviceScope() : outer(cur) { cur = this; }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+        cur = outer;
+    }
+    void pin(int device) {
+        int d = -1;
+        CK(cudaGetDevice(&d));
+        if (d == device) return;
+        CK(cudaSetDevice(device));
+        if (prev < 0) prev = d;
+    }
+};
+thread_local DeviceScope *DeviceScope::cur = nullptr;
+
+#define API_BEGIN                                                                                                      \
+    DeviceScope device_scope_;                                                                                         \
+    try {
 #define API_END                                                                                                        \
     }                                                                                                                  \
     catch (const Error &e) {                                                                                           \
@@ -1274,7 +1308,9 @@ using namespace csmc;
 
 static Ctx &ctx_of(void *c) {
     require(c != nullptr, CSMC_ERR_INVALID, "context is NULL");
-    return *static_cast<Ctx *>(c);
+    Ctx &C = *static_cast<Ctx *>(c);
+    if (DeviceScope::cur) DeviceScope::cur->pin(C.device);
+    return C;
 }
 
 extern "C" {
@@ -1328,7 +1364,7 @@ int csmc_create_batch(const csmc_lattice_desc *descs, int32_t n, const int32_t *
 int csmc_destroy(void *c) {
     API_BEGIN
     if (c) {
-        Ctx *C = static_cast<Ctx *>(c);
+        Ctx *C = &ctx_of(c); // its device current: the stream and buffers belong to it
         cudaStreamSynchronize(C->st);
         delete C;
     }
@@ -1513,13 +1549,12 @@ int csmc_energy_diff(void *c, int32_t slot, int64_t n, const int64_t *sites, con
     System &S = *C.sys[C.sys_of_slot(slot)];
     for (int64_t q = 0; q < n; q++)
         require(sites[q] >= 0 && sites[q] < S.plan.N, CSMC_ERR_INVALID, "site index out of range");
-    const int r = download_i32(C.chain_of)[slot] - S.base;
     DevBuf<int64_t> ds;
     DevBuf<double> dn, de;
     ds.upload(sites, n);
     dn.upload(ns, 3 * n);
     de.alloc(n);
-    with_args(C, S, [&](auto &a) { launch_energy_diff(a, r, n, ds.p, dn.p, de.p, C.st); });
+    with_args(C, S, [&](auto &a) { launch_energy_diff(a, C.chain_of.p, slot, n, ds.p, dn.p, de.p, C.st); });
     sync_check(C);
     if (n) CK(cudaMemcpy(dE, de.p, n * sizeof(double), cudaMemcpyDeviceToHost));
     API_END
@@ -1551,15 +1586,12 @@ int energy_diff_staged(void *c, int32_t slot, int64_t n, const int64_t *sites, c
     for (int64_t q = 0; q < n; q++)
         require(sites[q] >= 0 && sites[q] < S.plan.N, CSMC_ERR_INVALID, "site index out of range");
     if (n == 0) return CSMC_OK;
-    int32_t chain = 0;
-    CK(cudaMemcpy(&chain, C.chain_of.p + slot, sizeof(int32_t), cudaMemcpyDeviceToHost));
-    const int r = chain - S.base;
     int64_t *d_sites = static_cast<int64_t *>(scratch);
     double *d_ns = reinterpret_cast<double *>(d_sites + n_max);
     double *d_dE = d_ns + 3 * n_max;
     CK(cudaMemcpyAsync(d_sites, sites, n * sizeof(int64_t), cudaMemcpyHostToDevice, C.st));
     CK(cudaMemcpyAsync(d_ns, ns, 3 * n * sizeof(double), cudaMemcpyHostToDevice, C.st));
-    with_args(C, S, [&](auto &a) { launch_energy_diff(a, r, n, d_sites, d_ns, d_dE, C.st); });
+    with_args(C, S, [&](auto &a) { launch_energy_diff(a, C.chain_of.p, slot, n, d_sites, d_ns, d_dE, C.st); });
     CK(cudaMemcpyAsync(dE, d_dE, n * sizeof(double), cudaMemcpyDeviceToHost, C.st));
     sync_check(C);
     API_END
@@ -1598,6 +1630,33 @@ int csmc_metropolis_sweep(void *c, int32_t kind, double *accepted) {
     Launches L;
     const uint64_t before = C.nsweeps;
     sweep_global(C, 1, kind, 0.0, false, L);
+    renorm_check(C, L, before);
+    sync_check(C);
+    if (accepted) {
+        std::vector<double> a = download_f64(C.last_acc, C.n_chains);
+        std::copy(a.begin(), a.end(), accepted);
+    }
+    API_END
+}
+
+int csmc_metropolis_sweep_at(void *c, int32_t kind, const double *T, int32_t n_T, double *accepted) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(kind >= 0 && kind <= CSMC_METROPOLIS_CONSTRAINT_ADAPTIVE, CSMC_ERR_INVALID, "unknown Metropolis kind");
+    require(T != nullptr && (n_T == 1 || n_T == C.n_chains), CSMC_ERR_INVALID,
+            "T must hold one temperature or one per slot");
+    for (int k = 0; k < n_T; k++) require(T[k] > 0, CSMC_ERR_INVALID, "temperatures must be > 0");
+    Launches L;
+    const uint64_t before = C.nsweeps;
+    if (n_T == 1) {
+        sweep_global(C, 1, kind, T[0], false, L);
+    } else { // this sweep at T[slot]; mc.T of every slot and the permutation stay as they are
+        const size_t bytes = (size_t)C.n_chains * sizeof(double);
+        CK(cudaMemcpyAsync(C.T_stash.p, C.T_slot.p, bytes, cudaMemcpyDeviceToDevice, C.st));
+        CK(cudaMemcpyAsync(C.T_slot.p, T, bytes, cudaMemcpyHostToDevice, C.st));
+        sweep_global(C, 1, kind, 0.0, false, L);
+        CK(cudaMemcpyAsync(C.T_slot.p, C.T_stash.p, bytes, cudaMemcpyDeviceToDevice, C.st));
+    }
     renorm_check(C, L, before);
     sync_check(C);
     if (accepted) {
@@ -1939,6 +1998,27 @@ int csmc_spin_length_drift(void *c, double *drift) {
     float f;
     std::memcpy(&f, &bits, sizeof(f));
     *drift = f;
+    API_END
+}
+
+int csmc_debug_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out) {
+    API_BEGIN
+    require(n >= 0 && (n == 0 || (ctr && key && out)), CSMC_ERR_INVALID, "NULL argument");
+    if (n == 0) return CSMC_OK;
+    DevBuf<uint32_t> dc, dk, dout;
+    dc.upload(ctr, 4 * n);
+    dk.upload(key, 2 * n);
+    dout.alloc(4 * n);
+    launch_philox(dc.p, dk.p, n, dout.p, 0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out, dout.p, 4 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    API_END
+}
+
+int csmc_debug_device_allocs(int64_t *count) {
+    API_BEGIN
+    require(count != nullptr, CSMC_ERR_INVALID, "count is NULL");
+    *count = g_device_allocs.load();
     API_END
 }
 

@@ -8,6 +8,8 @@
 // The physics per site restates hamiltonian.jl, metropolis.jl and
 // monte_carlo.jl (see device.cuh).  Colour classes make every update within
 // a class independent, so each class is one parallel step.
+#include <cstdlib>
+
 #include "kernels.cuh"
 #include "launch.hpp"
 #include "reduce.cuh"
@@ -505,9 +507,12 @@ template <typename R, bool CUB, bool QUA> __global__ void k_local_field(SysArgs<
     out[3 * i + 2] = (double)H.z;
 }
 
+// The replica in `slot` is looked up on the device (chain_of), so the call
+// needs no device-to-host read before the launch.
 template <typename R, bool CUB, bool QUA>
-__global__ void k_energy_diff(SysArgs<R> a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE) {
-    const Spins<R> p = replica(a, r);
+__global__ void k_energy_diff(SysArgs<R> a, const int32_t *chain_of, int slot, int64_t n, const int64_t *sites,
+                              const double *ns, double *dE) {
+    const Spins<R> p = replica(a, chain_of[slot] - a.chain_base);
     const int64_t q = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (q >= n) return;
     const int64_t d = a.ref2dev[sites[q]];
@@ -544,6 +549,23 @@ template <typename R> __global__ void k_drift(SysArgs<R> a, unsigned int *bits) 
     atomicMax(bits, __float_as_uint(e));
 }
 
+// Philox4x32-10 blocks of n (counter, key) pairs: the generator the sweep
+// kernels draw from, exposed for its published known-answer vectors.
+__global__ void k_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out) {
+    const int64_t q = (int64_t)blockIdx.x * GB + threadIdx.x;
+    if (q >= n) return;
+    const U4 w = philox4x32_10(ctr[4 * q], ctr[4 * q + 1], ctr[4 * q + 2], ctr[4 * q + 3], key[2 * q], key[2 * q + 1]);
+    out[4 * q] = w.x;
+    out[4 * q + 1] = w.y;
+    out[4 * q + 2] = w.z;
+    out[4 * q + 3] = w.w;
+}
+
+void launch_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out, cudaStream_t st) {
+    if (n <= 0) return;
+    k_philox<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(ctr, key, n, out);
+}
+
 // ------------------------------------------------------------ launchers
 
 template <typename R> static dim3 grid_for(int64_t n, int chains) {
@@ -558,9 +580,22 @@ template <typename R> static dim3 grid_for(int64_t n, int chains) {
         else KERNEL<R, false, false> __VA_ARGS__;                                                                      \
     } while (0)
 
+// Programmatic stream serialization is left off in a process with a tool
+// injected (CUDA_INJECTION64_PATH: kernel profilers), which serialise and
+// intercept every launch; the kernels then run as ordinary launches, with the
+// same results (their griddepcontrol.wait does nothing).
+static bool pdl_allowed() {
+    static const bool ok = std::getenv("CUDA_INJECTION64_PATH") == nullptr;
+    return ok;
+}
+
 // A launch with programmatic stream serialization (see pdl_wait).
 template <typename... KArgs, typename... Args>
 static void launch_dep_b(void (*kern)(KArgs...), dim3 g, int block, cudaStream_t st, Args... args) {
+    if (!pdl_allowed()) {
+        kern<<<g, block, 0, st>>>(static_cast<KArgs>(args)...);
+        return;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = g;
     cfg.blockDim = dim3(block);
@@ -671,11 +706,11 @@ template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double
     DISPATCH_CQ(a, k_local_field, <<<g, GB, 0, st>>>(a, r, out));
 }
 template <typename R>
-void launch_energy_diff(const SysArgs<R> &a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE,
-                        cudaStream_t st) {
+void launch_energy_diff(const SysArgs<R> &a, const int32_t *chain_of, int slot, int64_t n, const int64_t *sites,
+                        const double *ns, double *dE, cudaStream_t st) {
     if (n <= 0) return;
     dim3 g = grid_for<R>(n, 1);
-    DISPATCH_CQ(a, k_energy_diff, <<<g, GB, 0, st>>>(a, r, n, sites, ns, dE));
+    DISPATCH_CQ(a, k_energy_diff, <<<g, GB, 0, st>>>(a, chain_of, slot, n, sites, ns, dE));
 }
 template <typename R> void launch_renorm(const SysArgs<R> &a, int chain_lo, int n_chains, cudaStream_t st) {
     k_renorm<R><<<grid_for<R>(a.tb.Np, n_chains), GB, 0, st>>>(a, chain_lo);
@@ -697,8 +732,8 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
     template void launch_gather<R>(const SysArgs<R> &, const int32_t *, int, int, double *, cudaStream_t);            \
     template void launch_random_spins<R>(const SysArgs<R> &, uint32_t, uint32_t, cudaStream_t);                       \
     template void launch_local_field<R>(const SysArgs<R> &, int, double *, cudaStream_t);                             \
-    template void launch_energy_diff<R>(const SysArgs<R> &, int, int64_t, const int64_t *, const double *, double *,  \
-                                        cudaStream_t);                                                                 \
+    template void launch_energy_diff<R>(const SysArgs<R> &, const int32_t *, int, int64_t, const int64_t *,          \
+                                        const double *, double *, cudaStream_t);                                       \
     template void launch_renorm<R>(const SysArgs<R> &, int, int, cudaStream_t);                                       \
     template void launch_drift<R>(const SysArgs<R> &, unsigned int *, cudaStream_t);
 

@@ -45,9 +45,10 @@ void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first,
                    cudaStream_t st);
 template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st);
 template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st);
+// energy differences on the replica in `slot` (looked up in chain_of on the device)
 template <typename R>
-void launch_energy_diff(const SysArgs<R> &a, int r, int64_t n, const int64_t *sites, const double *ns, double *dE,
-                        cudaStream_t st);
+void launch_energy_diff(const SysArgs<R> &a, const int32_t *chain_of, int slot, int64_t n, const int64_t *sites,
+                        const double *ns, double *dE, cudaStream_t st);
 template <typename R> void launch_renorm(const SysArgs<R> &a, int chain_lo, int n_chains, cudaStream_t st);
 template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits, cudaStream_t st);
 template <typename R>
@@ -61,6 +62,8 @@ template <typename R> int resident_capacity(int block, size_t smem, const Reside
 template <typename R>
 void launch_structure_factor(const SysArgs<R> &a, const R *pos, const R *ks, int64_t n_k, const int32_t *slot_of,
                              int slot_base, double *out, cudaStream_t st);
+// Philox4x32-10 of n counters (4 words each) under n keys (2 words each)
+void launch_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out, cudaStream_t st);
 // a kernel whose bounded wait cannot complete (see csmc_selftest_timeout)
 cudaError_t launch_wait_selftest(int which, unsigned int *ctr, int *error_flag, cudaStream_t st);
 // static shared memory of the selected resident kernel in bytes (-1: query failed)

@@ -131,6 +131,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *ctr, unsigned int n_b
 }
 
 // ---- thread-block cluster primitives
+// Hardware barrier of every thread of the cluster.  Its wait cannot be
+// bounded; it is used only at points that every rank of a cluster reaches the
+// same number of times (every decision to leave a loop is made cluster-wide,
+// see cluster_all), and the ranks of a cluster are co-scheduled, so it ends.
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
@@ -173,6 +177,28 @@ __device__ __forceinline__ V3<float> cluster_spin(uint32_t a, uint32_t, float) {
 }
 __device__ __forceinline__ V3<double> cluster_spin(uint32_t a, uint32_t comp, double) {
     return {ld_cluster(a, 0.0), ld_cluster(a + comp, 0.0), ld_cluster(a + 2 * comp, 0.0)};
+}
+
+__device__ __forceinline__ uint32_t ld_cluster_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+// Cluster-wide AND of a block-uniform flag: every rank publishes its flag in
+// `vote` (a shared word of each CTA), all ranks meet, read every rank's word,
+// and meet again before the word can be reused.  All ranks return the same
+// value, so a loop left on it is left by the whole cluster together: no rank
+// exits while a peer can still read its shared memory or arrive on its
+// barriers.
+template <int CL> __device__ __forceinline__ bool cluster_all(bool ok, uint32_t *vote) {
+    if (CL == 1) return ok;
+    if (threadIdx.x == 0) *vote = ok ? 1u : 0u;
+    cluster_sync_all();
+    uint32_t all = 1u;
+#pragma unroll
+    for (int q = 0; q < CL; q++) all &= ld_cluster_u32(map_rank(smem_u32(vote), (uint32_t)q));
+    cluster_sync_all();
+    return all != 0u;
 }
 
 // Remote arrive on the mbarrier at shared::cluster address `a` (release at
@@ -667,9 +693,10 @@ __global__ void __launch_bounds__(NT, 1)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t bar;
     __shared__ double scratch[32];
-    __shared__ double red[4];
+    __shared__ double red[3];
     __shared__ int s_item;
     __shared__ int s_ok;
+    __shared__ uint32_t s_vote;
     __shared__ double s_sigma, s_T;
     __shared__ R s_invT;
     __shared__ ResSys<R> s_sys;
@@ -756,15 +783,7 @@ __global__ void __launch_bounds__(NT, 1)
         const bool ok = mbar_wait_bounded(&bar, parity, cs.error_flag);
         parity ^= 1;
         const bool local_fail = __syncthreads_or(!ok); // block-uniform
-        bool fail = local_fail;
-        if (CL > 1) { // cluster-uniform: any rank failed
-            if (threadIdx.x == 0) red[3] = local_fail ? 1.0 : 0.0;
-            cluster_sync_all();
-            double n_fail = 0.0;
-            for (int q = 0; q < CL; q++) n_fail += ld_cluster(map_rank(smem_u32(&red[3]), q), 0.0);
-            cluster_sync_all();
-            fail = n_fail > 0.0;
-        }
+        const bool fail = !cluster_all<CL>(!local_fail, &s_vote); // cluster-uniform: any rank failed
         if (fail) {
             if (local_fail) mbar_wait_bounded(&bar, parity ^ 1, cs.error_flag); // copies still in flight
             __syncthreads();
@@ -874,7 +893,9 @@ __global__ void __launch_bounds__(NT, 1)
             if (!rd.persistent || !rd.swap_enabled || last % rd.swap_period != 0) break;
             // exchange of every lattice by block 0 between two grid barriers,
             // then the probe record of the exchange iteration
-            if (!grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok)) break;
+            // a barrier that gave up (timeout, or another CTA's error) ends the
+            // launch; the ranks of a cluster decide together
+            if (!cluster_all<CL>(grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok), &s_vote)) break;
             if (blockIdx.x == 0) {
                 for (int L = 0; L < rd.n_lattices; L++)
                     exchange_slots(cs, L, rd.lattices[L].x, rd.lattices[L].y, last, rd.swap_rate, rd.k0, rd.k1);
@@ -886,7 +907,7 @@ __global__ void __launch_bounds__(NT, 1)
                             record_slots(cs, rd.lattices[L].x, rd.lattices[L].y, rd.rec_E, rd.rec_M, kq, rd.n_slots);
                 }
             }
-            if (!grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok)) break;
+            if (!cluster_all<CL>(grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok), &s_vote)) break;
         }
         // every thread's shared-memory accesses are ordered before the bulk
         // copies that follow (the stores below, the next item's staging)

@@ -129,12 +129,29 @@ class Lattice:
     def desc(self) -> Description:
         return self._desc
 
+    @property
+    def spins(self) -> np.ndarray:
+        """lattice.spins (lattice.jl:73), 3 x N.  A MonteCarlo that swept this
+        lattice on the device leaves a pending read here (``_pull``); the
+        configuration is copied back on first access, not after every sweep."""
+        pull = self.__dict__.get("_pull")
+        if pull is not None:
+            self.__dict__["_pull"] = None
+            self.__dict__["_spins"] = pull()
+        return self.__dict__["_spins"]
+
+    @spins.setter
+    def spins(self, value) -> None:
+        self.__dict__["_pull"] = None
+        self.__dict__["_spins"] = value
+
     def __deepcopy__(self, memo):
         """deepcopy(lattice) (monte_carlo.jl:74): the ctypes description is rebuilt, not copied."""
         new = Lattice.__new__(Lattice)
         memo[id(self)] = new
+        _ = self.spins  # a pending device read is resolved before copying
         for k, v in self.__dict__.items():
-            if k in ("_desc", "_ctx", "_tables", "info"):
+            if k in ("_desc", "_ctx", "_tables", "info", "_pull"):
                 continue
             setattr(new, k, copy.deepcopy(v, memo))
         new._desc = Description(new.unit_cell, new.shape, new.S, new.bc)

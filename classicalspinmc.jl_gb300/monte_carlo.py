@@ -5,7 +5,7 @@ hamiltonian.jl and observables.jl on top of the GPU library.
 lattice's flattened tables and one replica per temperature: ``T`` may be a
 single temperature (the reference's one MPI rank) or a sequence (the ranks of
 a parallel-tempering ladder, batched on the one GPU).  Spins live on the
-device; ``mc.lattice.spins`` is refreshed after every driver call.
+device; ``mc.lattice.spins`` follows the device after every driver call (read back on access).
 
 The sweep plug point of the reference, ``alg(mc, T)``
 (``alg::FunctionWrapper{Float64,Tuple{MonteCarlo,Float64}}``, metropolis.jl:181-199),
@@ -293,15 +293,22 @@ class MonteCarlo:
             self.lattice.spins[:] = spins
 
     def sync(self) -> None:
-        self.lattice.spins = self.ctx.get_spins(0)
+        """mc.lattice.spins follows slot 0 on the device: read back when next accessed."""
+        ctx = self.ctx
+        self.lattice.__dict__["_pull"] = lambda: ctx.get_spins(0)
 
     # -- plug point ---------------------------------------------------------
     def _metropolis(self, kind: int, T=None):
-        if T is not None and self.n_replicas == 1 and float(T) != self.temperatures[0]:
-            self.temperatures[0] = float(T)
-            self.ctx.set_temperatures(self.temperatures)
+        """alg(mc, T): one sweep of every slot.  T (a number, or one per slot)
+        is the temperature of this sweep, as simulated_annealing! passes the
+        schedule's T (monte_carlo.jl:172-182); mc.T stays as it is."""
         acc = np.zeros(self.n_replicas)
-        self.ctx.call("csmc_metropolis_sweep", int(kind), _lib.ptr(acc, C.c_double))
+        if T is None:
+            self.ctx.call("csmc_metropolis_sweep", int(kind), _lib.ptr(acc, C.c_double))
+        else:
+            Ts = np.ascontiguousarray(np.atleast_1d(np.asarray(T, dtype=np.float64)))
+            self.ctx.call("csmc_metropolis_sweep_at", int(kind), _lib.ptr(Ts, C.c_double), len(Ts),
+                          _lib.ptr(acc, C.c_double))
         self.sync()
         return float(acc[0]) if self.n_replicas == 1 else acc
 

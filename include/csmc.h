@@ -266,6 +266,13 @@ int csmc_magnetization(void *ctx, double *M);
  * Philox counter (p, sweep, chain, 5) and (u_phi, u_z) from (p, sweep, chain,
  * 6) for proposal p.  accepted[n_slots] (or NULL) receives the accepted count. */
 int csmc_metropolis_sweep(void *ctx, int32_t kind, double *accepted);
+/* alg(mc, T) with the temperature the caller passes, as simulated_annealing!
+ * calls it with the schedule's T rather than mc.T (monte_carlo.jl:172-182;
+ * the FunctionWrapper signature of metropolis.jl:181-199 carries T).  n_T = 1:
+ * every slot sweeps at T[0]; n_T = n_slots: slot k sweeps at T[k].  The
+ * slots' own temperatures (csmc_set_temperatures) and the slot permutation
+ * are left unchanged.  Otherwise as csmc_metropolis_sweep. */
+int csmc_metropolis_sweep_at(void *ctx, int32_t kind, const double *T, int32_t n_T, double *accepted);
 /* overrelaxation! (monte_carlo.jl:126-139) on every slot. */
 int csmc_overrelax_sweep(void *ctx);
 /* deterministic_updates! (monte_carlo.jl:201-213) as n_sweeps colour sweeps
@@ -366,6 +373,18 @@ int csmc_autotune(void *ctx, const csmc_run_params *params, int32_t n_windows, c
 int csmc_set_renormalize(void *ctx, int32_t every_sweeps);
 /* max over sites and slots of ||s_i| - S| / S. */
 int csmc_spin_length_drift(void *ctx, double *drift);
+
+/* Philox4x32-10 (Salmon et al., SC'11), the counter-based generator every
+ * random draw of the sweep kernels comes from, evaluated by a device kernel
+ * on the current device: out[4q..4q+3] = Philox(ctr[4q..4q+3], key[2q..2q+1])
+ * for q < n.  A diagnostic of this library (its published known-answer
+ * vectors); no counterpart in the reference, which draws from Julia's
+ * default task RNG. */
+int csmc_debug_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out);
+/* Device allocations (cudaMalloc calls) the library has made in this process
+ * so far, over all contexts: a diagnostic of this library, no counterpart in
+ * the reference.  csmc_energy_diff_static leaves it unchanged. */
+int csmc_debug_device_allocs(int64_t *count);
 
 /* Device time (CUDA events on the context's stream) of the last csmc_run /
  * csmc_anneal call and the number of kernel launches it issued; of those, the

@@ -74,6 +74,27 @@ def test_philox_stream_properties(orc):
     assert orc.philox((0, 0, 0, 0), (0, 0)) != orc.philox((1, 0, 0, 0), (0, 0))
 
 
+# Known-answer vectors of Philox4x32-10 published with the algorithm (Salmon,
+# Moraes, Dror, Shaw, SC'11; the Random123 distribution's kat_vectors):
+# (counter, key) -> output, four 32-bit words each.
+PHILOX_KATS = [
+    ((0x00000000, 0x00000000, 0x00000000, 0x00000000), (0x00000000, 0x00000000),
+     (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+    ((0xffffffff, 0xffffffff, 0xffffffff, 0xffffffff), (0xffffffff, 0xffffffff),
+     (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+    ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+     (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+]
+
+
+def test_philox_known_answers(orc):
+    """The oracle's Philox4x32-10 (the stream the GPU replays decision for
+    decision in the colour-sweep parity tests) reproduces the published
+    known-answer vectors."""
+    for ctr, key, out in PHILOX_KATS:
+        assert orc.philox(ctr, key) == out
+
+
 def test_random_spins_on_sphere(m, orc):
     ol = orc.OracleLattice(m.examples.sc_heisenberg(), (3, 3, 3), 1.5)
     s = ol.random_spins(seed=3)

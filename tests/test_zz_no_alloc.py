@@ -76,3 +76,34 @@ def test_static_energy_diff_limits(m):
     code, _ = _energy_diff(ctx, "csmc_energy_diff_static", 0, np.zeros(n + 1, np.int64),
                            np.zeros((n + 1, 3)))
     assert code == 1 and b"CSMC_ENERGY_DIFF_STATIC_MAX" in ctx.lib.csmc_last_error()
+
+
+def _allocs(lib):
+    n = C.c_int64()
+    assert lib.csmc_debug_device_allocs(C.byref(n)) == 0
+    return n.value
+
+
+def test_static_energy_diff_allocates_nothing(m):
+    """Repeated calls make no device allocation (the library's own count of
+    cudaMalloc calls stays put), while the allocating entry point's calls are
+    counted; n = 0 is a no-op and a slot out of range is an error."""
+    lat = m.Lattice((6, 6), m.examples.triangular_afm(h=0.3), 1.0, rng=np.random.default_rng(7))
+    ctx = _Ctx(m, "fp32", lat, seed=8)
+    rng = np.random.default_rng(9)
+    sites = rng.integers(0, lat.size, 300).astype(np.int64)
+    new = np.ascontiguousarray(np.tile([0.6, 0.0, 0.8], (300, 1)))
+    c, first = _energy_diff(ctx, "csmc_energy_diff_static", 1, sites, new)
+    assert c == 0
+    before = _allocs(ctx.lib)
+    for _ in range(4):
+        c, again = _energy_diff(ctx, "csmc_energy_diff_static", 1, sites, new)
+        assert c == 0 and np.array_equal(again, first)
+    c, _ = _energy_diff(ctx, "csmc_energy_diff_static", 0, sites[:0], new[:0])
+    assert c == 0
+    assert _allocs(ctx.lib) == before
+    c, ref = _energy_diff(ctx, "csmc_energy_diff", 1, sites, new)
+    assert c == 0 and _allocs(ctx.lib) == before + 3  # sites, new spins and results staged
+    assert np.all(np.abs(first - ref) <= TOL["fp32"] * 2 * (6 + 0.3 + 1))
+    c, _ = _energy_diff(ctx, "csmc_energy_diff_static", 2, sites, new)  # two slots: 0 and 1
+    assert c == 1 and b"slot" in ctx.lib.csmc_last_error()
