@@ -96,6 +96,7 @@ SIGNATURES = {
     "csmc_set_spins_all": (C.c_int, [_vp, f64p]),
     "csmc_get_spins_all": (C.c_int, [_vp, f64p]),
     "csmc_random_spins": (C.c_int, [_vp, C.c_uint64]),
+    "csmc_set_chain_ids": (C.c_int, [_vp, u32p]),
     "csmc_set_temperatures": (C.c_int, [_vp, f64p]),
     "csmc_set_sigma": (C.c_int, [_vp, f64p]),
     "csmc_get_sigma": (C.c_int, [_vp, f64p]),

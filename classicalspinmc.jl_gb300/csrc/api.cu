@@ -118,6 +118,8 @@ struct Ctx {
     DevBuf<int32_t> slot_of, chain_of;
     DevBuf<double> T_slot, sigma_slot, acc_slot, exch_slot, E_chain, M_chain, last_acc;
     DevBuf<double> T_stash; // mc.T of every slot during a csmc_metropolis_sweep_at call
+    DevBuf<float> invT_slot, invT_stash; // (float)(1 / T) per slot (single-precision sweeps)
+    DevBuf<uint32_t> chain_id;           // per chain: the key of its Philox streams
     DevBuf<unsigned long long> sweep_acc;
     DevBuf<unsigned int> drift_bits;
     DevBuf<int> error_flag, work_ctr;
@@ -530,6 +532,14 @@ static void upload_resident(Ctx &C) {
     C.n_items = (int)items.size();
 }
 
+// (float)(1 / T[k]): the reciprocal temperatures the single-precision sweeps
+// multiply by, rounded once from the FP64 quotient
+static std::vector<float> reciprocals(const double *T, int n) {
+    std::vector<float> v((size_t)n);
+    for (int k = 0; k < n; k++) v[k] = (float)(1.0 / T[k]);
+    return v;
+}
+
 static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, int precision, uint64_t seed) {
     require(n >= 1, CSMC_ERR_INVALID, "need at least one lattice");
     require(precision == CSMC_FP32 || precision == CSMC_FP64, CSMC_ERR_INVALID, "precision must be CSMC_FP32 or CSMC_FP64");
@@ -543,6 +553,10 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
         require(reps[k] >= 1, CSMC_ERR_INVALID, "replica count must be >= 1");
         auto S = std::make_unique<System>();
         S->plan = make_plan(&descs[k]);
+        const Plan &P = S->plan;
+        // the sweep kernels index the [slot][site] partner tables in 32 bits
+        require((int64_t)std::max({P.W2, 2 * P.W3, 3 * P.W4, 1}) * P.Np < ((int64_t)1 << 31), CSMC_ERR_UNSUPPORTED,
+                "lattice too large: partner slots x padded sites must stay below 2^31");
         S->R = reps[k];
         S->base = chains;
         chains += reps[k];
@@ -571,6 +585,9 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     std::vector<double> ones(nc, 1.0), sig(nc, 60.0), zeros(nc, 0.0);
     C->T_slot.upload(ones);
     C->T_stash.upload(ones);
+    std::vector<float> fones(nc, 1.0f);
+    C->invT_slot.upload(fones);
+    C->invT_stash.upload(fones);
     C->sigma_slot.upload(sig);
     C->acc_slot.upload(zeros);
     C->exch_slot.upload(zeros);
@@ -599,6 +616,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.slot_of = C->slot_of.p;
     cs.chain_of = C->chain_of.p;
     cs.T_slot = C->T_slot.p;
+    cs.invT_slot = C->invT_slot.p;
     cs.sigma_slot = C->sigma_slot.p;
     cs.acc_slot = C->acc_slot.p;
     cs.exch_slot = C->exch_slot.p;
@@ -607,6 +625,10 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.sweep_acc = C->sweep_acc.p;
     cs.drift_bits = C->drift_bits.p;
     cs.error_flag = C->error_flag.p;
+    std::vector<uint32_t> ids(nc);
+    std::iota(ids.begin(), ids.end(), 0u);
+    C->chain_id.upload(ids);
+    cs.chain_id = C->chain_id.p;
 
     std::vector<int2> lat;
     for (auto &S : C->sys) lat.push_back(make_int2(S->base, S->R));
@@ -1425,7 +1447,10 @@ int csmc_get_spins_all(void *c, double *spins) {
 int csmc_random_spins(void *c, uint64_t seed) {
     API_BEGIN
     Ctx &C = ctx_of(c);
-    for (auto &S : C.sys) with_args(C, *S, [&](auto &a) { launch_random_spins(a, (uint32_t)seed, (uint32_t)(seed >> 32), C.st); });
+    for (auto &S : C.sys)
+        with_args(C, *S, [&](auto &a) {
+            launch_random_spins(a, C.chain_id.p, (uint32_t)seed, (uint32_t)(seed >> 32), C.st);
+        });
     sync_check(C);
     API_END
 }
@@ -1436,6 +1461,8 @@ int csmc_set_temperatures(void *c, const double *T) {
     require(T != nullptr, CSMC_ERR_INVALID, "T is NULL");
     for (int k = 0; k < C.n_chains; k++) require(T[k] > 0, CSMC_ERR_INVALID, "temperatures must be > 0");
     CK(cudaMemcpy(C.T_slot.p, T, C.n_chains * sizeof(double), cudaMemcpyHostToDevice));
+    const std::vector<float> inv = reciprocals(T, C.n_chains);
+    CK(cudaMemcpy(C.invT_slot.p, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice));
     std::vector<int32_t> ident(C.n_chains);
     std::iota(ident.begin(), ident.end(), 0);
     CK(cudaMemcpy(C.slot_of.p, ident.data(), ident.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
@@ -1651,11 +1678,16 @@ int csmc_metropolis_sweep_at(void *c, int32_t kind, const double *T, int32_t n_T
     if (n_T == 1) {
         sweep_global(C, 1, kind, T[0], false, L);
     } else { // this sweep at T[slot]; mc.T of every slot and the permutation stay as they are
-        const size_t bytes = (size_t)C.n_chains * sizeof(double);
+        const size_t bytes = (size_t)C.n_chains * sizeof(double), fbytes = (size_t)C.n_chains * sizeof(float);
+        const std::vector<float> inv = reciprocals(T, C.n_chains);
         CK(cudaMemcpyAsync(C.T_stash.p, C.T_slot.p, bytes, cudaMemcpyDeviceToDevice, C.st));
+        CK(cudaMemcpyAsync(C.invT_stash.p, C.invT_slot.p, fbytes, cudaMemcpyDeviceToDevice, C.st));
         CK(cudaMemcpyAsync(C.T_slot.p, T, bytes, cudaMemcpyHostToDevice, C.st));
+        CK(cudaMemcpyAsync(C.invT_slot.p, inv.data(), fbytes, cudaMemcpyHostToDevice, C.st));
         sweep_global(C, 1, kind, 0.0, false, L);
         CK(cudaMemcpyAsync(C.T_slot.p, C.T_stash.p, bytes, cudaMemcpyDeviceToDevice, C.st));
+        CK(cudaMemcpyAsync(C.invT_slot.p, C.invT_stash.p, fbytes, cudaMemcpyDeviceToDevice, C.st));
+        CK(cudaStreamSynchronize(C.st)); // the host copy of the reciprocals is read before it goes
     }
     renorm_check(C, L, before);
     sync_check(C);
@@ -1998,6 +2030,15 @@ int csmc_spin_length_drift(void *c, double *drift) {
     float f;
     std::memcpy(&f, &bits, sizeof(f));
     *drift = f;
+    API_END
+}
+
+int csmc_set_chain_ids(void *c, const uint32_t *ids) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(ids != nullptr, CSMC_ERR_INVALID, "ids is NULL");
+    CK(cudaStreamSynchronize(C.st));
+    CK(cudaMemcpy(C.chain_id.p, ids, C.n_chains * sizeof(uint32_t), cudaMemcpyHostToDevice));
     API_END
 }
 

@@ -172,7 +172,8 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     hb = {R(0), R(0), R(0)};
     hc = {R(0), R(0), R(0)};
     hq = {R(0), R(0), R(0)};
-    const int64_t Np = tb.Np;
+    // 32-bit table offsets: the host admits lattices with W * Np < 2^31
+    const int Np = (int)tb.Np, di = (int)d;
     // one term of each kind, its partner spins given
     auto bil = [&](int t, V3<R> sj) {
         const int id = cf.c2[b * tb.W2 + t];
@@ -237,45 +238,45 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     if (kPairs) { // bilinear terms in threes
         constexpr int G = 3;
         for (; t + G <= tb.W2; t += G) {
-            int64_t j[G];
+            int j[G];
             V3<R> sj[G];
 #pragma unroll
-            for (int u = 0; u < G; u++) j[u] = tb.p2[(t + u) * Np + d];
+            for (int u = 0; u < G; u++) j[u] = (int)tb.p2[(t + u) * Np + di];
 #pragma unroll
             for (int u = 0; u < G; u++) sj[u] = sv.get(j[u]);
 #pragma unroll
             for (int u = 0; u < G; u++) bil(t + u, sj[u]);
         }
     }
-    for (; t < tb.W2; t++) bil(t, sv.get(tb.p2[t * Np + d]));
+    for (; t < tb.W2; t++) bil(t, sv.get(tb.p2[t * Np + di]));
     if (CUB) {
         t = 0;
         if (kPairs)
             for (; t + 2 <= tb.W3; t += 2) {
-                const int64_t j0 = tb.p3[(2 * t) * Np + d], k0 = tb.p3[(2 * t + 1) * Np + d];
-                const int64_t j1 = tb.p3[(2 * t + 2) * Np + d], k1 = tb.p3[(2 * t + 3) * Np + d];
+                const int j0 = (int)tb.p3[(2 * t) * Np + di], k0 = (int)tb.p3[(2 * t + 1) * Np + di];
+                const int j1 = (int)tb.p3[(2 * t + 2) * Np + di], k1 = (int)tb.p3[(2 * t + 3) * Np + di];
                 const V3<R> sj0 = sv.get(j0), sk0 = sv.get(k0), sj1 = sv.get(j1), sk1 = sv.get(k1);
                 cub(t, sj0, sk0);
                 cub(t + 1, sj1, sk1);
             }
-        for (; t < tb.W3; t++) cub(t, sv.get(tb.p3[(2 * t) * Np + d]), sv.get(tb.p3[(2 * t + 1) * Np + d]));
+        for (; t < tb.W3; t++) cub(t, sv.get(tb.p3[(2 * t) * Np + di]), sv.get(tb.p3[(2 * t + 1) * Np + di]));
     }
     if (QUA) {
         t = 0;
         if (kPairs)
             for (; t + 2 <= tb.W4; t += 2) {
-                const int64_t j0 = tb.p4[(3 * t) * Np + d], k0 = tb.p4[(3 * t + 1) * Np + d],
-                              l0 = tb.p4[(3 * t + 2) * Np + d];
-                const int64_t j1 = tb.p4[(3 * t + 3) * Np + d], k1 = tb.p4[(3 * t + 4) * Np + d],
-                              l1 = tb.p4[(3 * t + 5) * Np + d];
+                const int j0 = (int)tb.p4[(3 * t) * Np + di], k0 = (int)tb.p4[(3 * t + 1) * Np + di],
+                              l0 = (int)tb.p4[(3 * t + 2) * Np + di];
+                const int j1 = (int)tb.p4[(3 * t + 3) * Np + di], k1 = (int)tb.p4[(3 * t + 4) * Np + di],
+                              l1 = (int)tb.p4[(3 * t + 5) * Np + di];
                 const V3<R> sj0 = sv.get(j0), sk0 = sv.get(k0), sl0 = sv.get(l0);
                 const V3<R> sj1 = sv.get(j1), sk1 = sv.get(k1), sl1 = sv.get(l1);
                 qua(t, sj0, sk0, sl0);
                 qua(t + 1, sj1, sk1, sl1);
             }
         for (; t < tb.W4; t++)
-            qua(t, sv.get(tb.p4[(3 * t) * Np + d]), sv.get(tb.p4[(3 * t + 1) * Np + d]),
-                sv.get(tb.p4[(3 * t + 2) * Np + d]));
+            qua(t, sv.get(tb.p4[(3 * t) * Np + di]), sv.get(tb.p4[(3 * t + 1) * Np + di]),
+                sv.get(tb.p4[(3 * t + 2) * Np + di]));
     }
 }
 

@@ -33,41 +33,49 @@ template <typename R> __device__ __forceinline__ Spins<R> replica(const SysArgs<
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 template <typename R, bool CUB, bool QUA>
-__global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs, int64_t start, int64_t count,
-                                                     int chain_lo, int kind, uint32_t msweep, double T_override) {
+__global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs, int start, int count, int chain_lo,
+                                                     int kind, uint32_t msweep, double T_override,
+                                                     float invT_override) {
     pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const int c = a.chain_base + r;
     const Spins<R> p = replica(a, r);
-    // T, 1/T and sigma formed once per block: FP64 arithmetic -- even one
-    // comparison per thread -- runs at a small fraction of the FP32 rate on
-    // this device
+    // 1/T and sigma of the block's replica.  Single precision reads 1/T
+    // formed on the host (FP64 arithmetic -- even one division or comparison
+    // per block -- runs at a small fraction of the FP32 rate on this device);
+    // double precision divides by T itself.
     __shared__ R s_invT, s_sigma;
     __shared__ double s_T;
+    __shared__ uint32_t s_key;
     if (threadIdx.x == 0) {
         const int slot = cs.slot_of[c];
-        const double T = T_override > 0 ? T_override : cs.T_slot[slot];
-        s_T = T;
-        s_invT = (R)(1.0 / T);
+        s_key = cs.chain_id[c];
+        if constexpr (sizeof(R) == 4) {
+            s_invT = invT_override > 0.f ? invT_override : cs.invT_slot[slot];
+        } else {
+            s_T = T_override > 0 ? T_override : cs.T_slot[slot];
+            s_invT = (R)(1.0 / s_T);
+        }
         s_sigma = (R)cs.sigma_slot[slot];
     }
     __syncthreads();
     const R invT = s_invT, sigma = s_sigma;
-    const double T = s_T; // used by the double-precision acceptance only
-    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    const uint32_t key = s_key; // the replica's Philox stream key
+    const double T = sizeof(R) == 4 ? 0.0 : s_T; // used by the double-precision acceptance only
+    const int i = (int)blockIdx.x * GB + (int)threadIdx.x;
     unsigned acc = 0;
     if (i < count) {
-        const int64_t d = start + i;
+        const int d = start + i;
         const int b = a.tb.pat[d];
         V3<R> hb, hc, hq;
         partner_fields<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b, hb, hc, hq);
         const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
         const V3<R> s = p.get(d);
-        const Draw<R> dr((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1);
+        const Draw<R> dr((uint32_t)d, msweep, key, a.k0, a.k1);
         const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
         const R dE = delta_e<R>(a.cf, b, s, sn, hext);
         bool accept = dE < R(0);
-        if (!accept) accept = dr.acc((uint32_t)d, msweep, (uint32_t)c, a.k0, a.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
+        if (!accept) accept = dr.acc((uint32_t)d, msweep, key, a.k0, a.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
         if (accept) {
             p.set(d, sn);
             acc = 1;
@@ -125,6 +133,7 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
                                                         uint32_t msweep, double T_override) {
     const int r = blockIdx.x;
     const int c = a.chain_base + r;
+    const uint32_t key = cs.chain_id[c];
     const Spins<R> p = replica(a, r);
     double vx, vy, vz;
     constraint_v_sum(a, p, k, vx, vy, vz);
@@ -144,11 +153,11 @@ __global__ void __launch_bounds__(32) k_metro_constraint(SysArgs<R> a, ChainStat
     const uint64_t n = (uint64_t)a.n_real;
     // the draws of proposal q + 1 are computed while proposal q waits for its
     // spins (they depend on nothing the proposal changes)
-    U4 A = philox4x32_10(0u, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
-    U4 B = philox4x32_10(0u, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+    U4 A = philox4x32_10(0u, msweep, key, PURPOSE_CONS_A, a.k0, a.k1);
+    U4 B = philox4x32_10(0u, msweep, key, PURPOSE_CONS_B, a.k0, a.k1);
     for (uint64_t q = 0; q < n; q++) {
-        const U4 An = philox4x32_10((uint32_t)(q + 1), msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
-        const U4 Bn = philox4x32_10((uint32_t)(q + 1), msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+        const U4 An = philox4x32_10((uint32_t)(q + 1), msweep, key, PURPOSE_CONS_A, a.k0, a.k1);
+        const U4 Bn = philox4x32_10((uint32_t)(q + 1), msweep, key, PURPOSE_CONS_B, a.k0, a.k1);
         const int64_t i = (int64_t)(((uint64_t)A.x * n) >> 32);
         const int64_t d = a.ref2dev[i];
         const int b = a.tb.pat[d];
@@ -196,6 +205,7 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
     constexpr unsigned FULL = 0xffffffffu;
     const int r = blockIdx.x, lane = threadIdx.x;
     const int c = a.chain_base + r;
+    const uint32_t key = cs.chain_id[c];
     const Spins<R> p = replica(a, r);
     double vx, vy, vz;
     constraint_v_sum(a, p, k, vx, vy, vz);
@@ -224,8 +234,8 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
     int64_t pd = -1, pnb[CONS_NB];
     int pbs = 0;
     auto fetch = [&](uint64_t qq, U4 &A, U4 &B, int64_t &dd, int &bb, int64_t *nn) {
-        A = philox4x32_10((uint32_t)qq, msweep, (uint32_t)c, PURPOSE_CONS_A, a.k0, a.k1);
-        B = philox4x32_10((uint32_t)qq, msweep, (uint32_t)c, PURPOSE_CONS_B, a.k0, a.k1);
+        A = philox4x32_10((uint32_t)qq, msweep, key, PURPOSE_CONS_A, a.k0, a.k1);
+        B = philox4x32_10((uint32_t)qq, msweep, key, PURPOSE_CONS_B, a.k0, a.k1);
         dd = a.ref2dev[(int64_t)(((uint64_t)A.x * n) >> 32)];
         bb = a.tb.pat[dd];
 #pragma unroll
@@ -311,13 +321,13 @@ __global__ void __launch_bounds__(32) k_metro_constraint_batch(SysArgs<R> a, Cha
 
 // overrelaxation! body (monte_carlo.jl:128-137) on one colour class.
 template <typename R, bool CUB, bool QUA>
-__global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+__global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int start, int count, int chain_lo) {
     pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
-    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    const int i = (int)blockIdx.x * GB + (int)threadIdx.x;
     if (i >= count) return;
-    const int64_t d = start + i;
+    const int d = start + i;
     const int b = a.tb.pat[d];
     const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
@@ -326,13 +336,13 @@ __global__ void __launch_bounds__(GB) k_or_colour(SysArgs<R> a, int64_t start, i
 
 // deterministic_updates! body (monte_carlo.jl:205-210) on one colour class.
 template <typename R, bool CUB, bool QUA>
-__global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int64_t start, int64_t count, int chain_lo) {
+__global__ void __launch_bounds__(GB) k_det_colour(SysArgs<R> a, int start, int count, int chain_lo) {
     pdl_wait();
     const int r = chain_lo + blockIdx.y;
     const Spins<R> p = replica(a, r);
-    const int64_t i = (int64_t)blockIdx.x * GB + threadIdx.x;
+    const int i = (int)blockIdx.x * GB + (int)threadIdx.x;
     if (i >= count) return;
-    const int64_t d = start + i;
+    const int d = start + i;
     const int b = a.tb.pat[d];
     const V3<R> H = local_field<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, b);
     if (H.x == R(0) && H.y == R(0) && H.z == R(0)) return;
@@ -355,7 +365,7 @@ __global__ void __launch_bounds__(GB) k_energy_part(SysArgs<R> a, int chain_lo, 
     R acc = R(0);
 #pragma unroll 1
     for (int k = 0; k < RK; k++) {
-        const int64_t d = (int64_t)blockIdx.x * RB + k * GB + threadIdx.x;
+        const int d = (int)blockIdx.x * RB + k * GB + (int)threadIdx.x;
         if (d < a.tb.Np && a.dev2ref[d] >= 0)
             acc = Fp<R>::add(acc, site_energy_share<R, uint32_t, CUB, QUA>(a.tb, a.cf, p, d, a.tb.pat[d]));
     }
@@ -372,7 +382,7 @@ template <typename R> __global__ void __launch_bounds__(GB) k_magnet_part(SysArg
     R ax = R(0), ay = R(0), az = R(0);
 #pragma unroll 2
     for (int k = 0; k < RK; k++) {
-        const int64_t d = (int64_t)blockIdx.x * RB + k * GB + threadIdx.x;
+        const int d = (int)blockIdx.x * RB + k * GB + (int)threadIdx.x;
         if (d < a.tb.Np) { // padding holds zero spins
             const V3<R> s = p.get(d);
             ax = Fp<R>::add(ax, s.x);
@@ -478,14 +488,15 @@ __global__ void k_gather(SysArgs<R> a, const int32_t *chain_of, int slot_first, 
 }
 
 // Uniform spins from the INIT stream, counter (reference site, 0, chain, INIT).
-template <typename R> __global__ void k_random_spins(SysArgs<R> a, uint32_t k0, uint32_t k1) {
+template <typename R>
+__global__ void k_random_spins(SysArgs<R> a, const uint32_t *chain_id, uint32_t k0, uint32_t k1) {
     const int r = blockIdx.y;
     const Spins<R> p = replica(a, r);
     const int64_t d = (int64_t)blockIdx.x * GB + threadIdx.x;
     if (d >= a.tb.Np) return;
     const int64_t i = a.dev2ref[d];
     if (i < 0) return;
-    const U4 w = philox4x32_10((uint32_t)i, 0u, (uint32_t)(a.chain_base + r), PURPOSE_INIT, k0, k1);
+    const U4 w = philox4x32_10((uint32_t)i, 0u, chain_id[a.chain_base + r], PURPOSE_INIT, k0, k1);
     const double uphi = u53(w.x, w.y), uz = u53(w.z, w.w);
     double sp, cp;
     sincospi(2.0 * uphi, &sp, &cp);
@@ -621,26 +632,29 @@ static void launch_dep(void (*kern)(KArgs...), dim3 g, cudaStream_t st, Args... 
     ((a).cub && (a).qua ? KERNEL<R, true, true>                                                                       \
                         : (a).cub ? KERNEL<R, true, false> : (a).qua ? KERNEL<R, false, true> : KERNEL<R, false, false>)
 
+// (the host admits lattices of fewer than 2^31 / W device sites, so colour
+// class starts and counts fit 32 bits)
 template <typename R>
 void launch_metro_colour(const SysArgs<R> &a, const ChainState &cs, int64_t start, int64_t count, int chain_lo,
                          int n_chains, int kind, uint32_t msweep, double T_override, cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    launch_dep(PICK_CQ(a, k_metro_colour), grid_for<R>(count, n_chains), st, a, cs, start, count, chain_lo, kind,
-               msweep, T_override);
+    const float invT_override = T_override > 0 ? (float)(1.0 / T_override) : 0.f;
+    launch_dep(PICK_CQ(a, k_metro_colour), grid_for<R>(count, n_chains), st, a, cs, (int)start, (int)count, chain_lo,
+               kind, msweep, T_override, invT_override);
 }
 
 template <typename R>
 void launch_or_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
                       cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    launch_dep(PICK_CQ(a, k_or_colour), grid_for<R>(count, n_chains), st, a, start, count, chain_lo);
+    launch_dep(PICK_CQ(a, k_or_colour), grid_for<R>(count, n_chains), st, a, (int)start, (int)count, chain_lo);
 }
 
 template <typename R>
 void launch_det_colour(const SysArgs<R> &a, int64_t start, int64_t count, int chain_lo, int n_chains,
                        cudaStream_t st) {
     if (count <= 0 || n_chains <= 0) return;
-    launch_dep(PICK_CQ(a, k_det_colour), grid_for<R>(count, n_chains), st, a, start, count, chain_lo);
+    launch_dep(PICK_CQ(a, k_det_colour), grid_for<R>(count, n_chains), st, a, (int)start, (int)count, chain_lo);
 }
 
 int64_t partial_blocks(int64_t Np) { return (Np + RB - 1) / RB; }
@@ -698,8 +712,9 @@ void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first,
                    cudaStream_t st) {
     k_gather<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, dst);
 }
-template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st) {
-    k_random_spins<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, k0, k1);
+template <typename R>
+void launch_random_spins(const SysArgs<R> &a, const uint32_t *chain_id, uint32_t k0, uint32_t k1, cudaStream_t st) {
+    k_random_spins<R><<<grid_for<R>(a.tb.Np, a.n_rep), GB, 0, st>>>(a, chain_id, k0, k1);
 }
 template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st) {
     dim3 g = grid_for<R>(a.tb.Np, 1);
@@ -730,7 +745,7 @@ template <typename R> void launch_drift(const SysArgs<R> &a, unsigned int *bits,
     template void launch_magnet<R>(const SysArgs<R> &, const ChainState &, int, int, double *, cudaStream_t);         \
     template void launch_scatter<R>(const SysArgs<R> &, const int32_t *, int, int, const double *, cudaStream_t);     \
     template void launch_gather<R>(const SysArgs<R> &, const int32_t *, int, int, double *, cudaStream_t);            \
-    template void launch_random_spins<R>(const SysArgs<R> &, uint32_t, uint32_t, cudaStream_t);                       \
+    template void launch_random_spins<R>(const SysArgs<R> &, const uint32_t *, uint32_t, uint32_t, cudaStream_t);     \
     template void launch_local_field<R>(const SysArgs<R> &, int, double *, cudaStream_t);                             \
     template void launch_energy_diff<R>(const SysArgs<R> &, const int32_t *, int, int64_t, const int64_t *,          \
                                         const double *, double *, cudaStream_t);                                       \

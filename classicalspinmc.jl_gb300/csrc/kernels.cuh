@@ -15,11 +15,13 @@ struct ChainState {
     int32_t *slot_of;  // chain -> slot
     int32_t *chain_of; // slot -> chain
     double *T_slot, *sigma_slot;
+    float *invT_slot;  // (float)(1 / T) per slot, formed on the host
     double *acc_slot, *exch_slot;
     double *E_chain, *M_chain;
     unsigned long long *sweep_acc; // accepted proposals of the current sweep, per chain
     unsigned int *drift_bits;      // max relative |S| error, float bits
     int *error_flag;               // nonzero: a bounded wait gave up
+    const uint32_t *chain_id;      // per chain: the key of its Philox streams (default: the chain index)
 };
 
 // One lattice for the global-memory kernels.

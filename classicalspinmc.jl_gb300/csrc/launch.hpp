@@ -43,7 +43,9 @@ void launch_scatter(const SysArgs<R> &a, const int32_t *chain_of, int slot_first
 template <typename R>
 void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, double *dst,
                    cudaStream_t st);
-template <typename R> void launch_random_spins(const SysArgs<R> &a, uint32_t k0, uint32_t k1, cudaStream_t st);
+// uniform spins from the INIT stream of each replica's chain id
+template <typename R>
+void launch_random_spins(const SysArgs<R> &a, const uint32_t *chain_id, uint32_t k0, uint32_t k1, cudaStream_t st);
 template <typename R> void launch_local_field(const SysArgs<R> &a, int r, double *out, cudaStream_t st);
 // energy differences on the replica in `slot` (looked up in chain_of on the device)
 template <typename R>

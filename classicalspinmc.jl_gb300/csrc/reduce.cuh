@@ -55,4 +55,28 @@ template <typename T> __device__ __forceinline__ double block_sum_any(T v, doubl
     return block_sum_warps((double)warp_sum(v), scratch, (int)(blockDim.x >> 5));
 }
 
+// Four sums over a block of any multiple of 32 threads at once (one pass
+// through shared memory); results valid in thread 0.  scratch needs 4 x 32
+// doubles.  Same order per value as block_sum_any.
+template <typename T>
+__device__ __forceinline__ void block_sum4_any(T a, T b, T c, T d, double *scratch, double (&out)[4]) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
+    const double v[4] = {(double)warp_sum(a), (double)warp_sum(b), (double)warp_sum(c), (double)warp_sum(d)};
+    __syncthreads();
+    if (l == 0)
+#pragma unroll
+        for (int q = 0; q < 4; q++) scratch[q * 32 + w] = v[q];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        double t = 0.0;
+        if (threadIdx.x < 32) {
+            t = l < nw ? scratch[q * 32 + l] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        }
+        out[q] = t;
+    }
+}
+
 } // namespace csmc

@@ -201,23 +201,6 @@ template <int CL> __device__ __forceinline__ bool cluster_all(bool ok, uint32_t 
     return all != 0u;
 }
 
-// Remote arrive on the mbarrier at shared::cluster address `a` (release at
-// cluster scope: this CTA's shared-memory writes become visible to a thread
-// that then acquires the barrier phase).
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t a) {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok)
-                 : "r"(smem_u32(bar)), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-
 // Bytes of one site in shared memory per spin component block: 16 (float4
 // sites) or 8 (one double of a component block).
 template <typename R> constexpr uint32_t site_stride() { return sizeof(R) == 4 ? 16u : 8u; }
@@ -242,31 +225,15 @@ template <typename R> __host__ __device__ constexpr int64_t spin_smem_bytes(int6
 // Block (CL = 1) or cluster barrier and sums; totals valid in thread 0 of
 // every CTA, identical on all ranks (same summation order).
 template <int CL> struct Sync {
-    double *scratch, *red; // scratch: 32 doubles; red: 3 doubles (cluster exchange)
-    uint64_t *pbar;        // phase mbarrier of this CTA (CL arrivals per phase)
-    uint32_t *pphase;      // its current phase parity (thread 0)
+    double *scratch, *red; // scratch: 4 x 32 doubles; red: 4 doubles (cluster exchange)
     int *error_flag;
-    // Barrier across the cluster between colour classes: every CTA first
-    // waits for its own threads (bar.sync), then thread 0 arrives on every
-    // rank's phase mbarrier and waits, suspended in try_wait, for the
-    // arrivals of all ranks; bounded (one second), reporting a timeout
-    // through the error flag.
+    // Barrier between colour classes: the block, or every thread of the
+    // cluster (hardware cluster barrier, release/acquire at cluster scope, so
+    // each rank's shared-memory writes are visible to the others' reads after
+    // it).  Every rank runs the same colour loop, so all reach it.
     __device__ __forceinline__ void bar() const {
-        __syncthreads();
-        if (CL > 1) {
-            if (threadIdx.x == 0) {
-                const uint32_t a = smem_u32(pbar);
-#pragma unroll
-                for (int r = 0; r < CL; r++) mbar_arrive_cluster(map_rank(a, r));
-                const uint32_t ph = *pphase;
-                bool done = false;
-                const uint64_t t0 = gtimer_ns();
-                while (!done && gtimer_ns() - t0 < WAIT_BUDGET_NS) done = mbar_try_wait_cluster(pbar, ph);
-                if (!done) atomicExch(error_flag, 1);
-                *pphase = ph ^ 1u;
-            }
-            __syncthreads();
-        }
+        if (CL > 1) cluster_sync_all();
+        else __syncthreads();
     }
     template <typename T> __device__ double sum(T v) const {
         double t = block_sum_any(v, scratch);
@@ -278,6 +245,25 @@ template <int CL> struct Sync {
             for (int r = 0; r < CL; r++) tot += ld_cluster(map_rank(smem_u32(red), r), 0.0);
         cluster_sync_all();
         return tot;
+    }
+    // four totals at once (the energy and the magnetisation of a measuring sweep)
+    template <typename T> __device__ void sum4(T x0, T x1, T x2, T x3, double (&o)[4]) const {
+        block_sum4_any(x0, x1, x2, x3, scratch, o);
+        if (CL == 1) return;
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int q = 0; q < 4; q++) red[q] = o[q];
+        cluster_sync_all();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) o[q] = 0.0;
+            for (int r = 0; r < CL; r++) {
+                const uint32_t base = map_rank(smem_u32(red), r);
+#pragma unroll
+                for (int q = 0; q < 4; q++) o[q] += ld_cluster(base + 8 * q, 0.0);
+            }
+        }
+        cluster_sync_all();
     }
     template <typename T> __device__ void sum3(T x, T y, T z, double &a, double &b, double &c) const {
         a = block_sum_any(x, scratch);
@@ -308,7 +294,8 @@ template <typename R, int CL> struct ResidentCommon {
     const ResSys<R> &S;
     Spins<R> sp; // this CTA's sites in shared memory (local indices)
     Sync<CL> sy;
-    int c, slot, rank;
+    uint32_t key; // the replica's Philox stream key (its chain id)
+    int slot, rank;
     R *scoef;
 
     __device__ __forceinline__ int col_begin(int col) const {
@@ -380,15 +367,16 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
     static constexpr int kMaxThreads = 512; // 128 registers per thread
     static constexpr int kCoefSmem = 1;
     static constexpr bool kPartnerWords = false;
+    static constexpr bool kMeasuringSweep = false; // energy and |M| in separate passes
     using B = ResidentCommon<R, CL>;
-    using B::c;
+    using B::key;
     using B::S;
     using B::sp;
     Tab<uint16_t> tb;      // this rank's tables (local indices; CL = 1: the replica's)
     ClusterView<R, CL> cv; // partner spins
-    __device__ ResidentGeneric(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
-                               const uint4 *, bool)
-        : B{s, sp_, sy_, c_, slot_, rk, coef} {
+    __device__ ResidentGeneric(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, uint32_t key_, int slot_, int rk,
+                               R *coef, const uint4 *, bool)
+        : B{s, sp_, sy_, key_, slot_, rk, coef} {
         tb = S.tb;
         cv.sp = sp_;
         cv.comp = (uint32_t)(S.Npl * sizeof(double));
@@ -406,7 +394,8 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
     }
     __device__ void prepare() const {}
 
-    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
+    template <bool MEASURE = false>
+    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep, R * = nullptr) const {
         unsigned acc = 0;
         for (int col = 0; col < S.n_colours; col++) {
             const int st = this->col_begin(col), n = this->col_size(col);
@@ -418,11 +407,11 @@ template <typename R, bool CUB, bool QUA, int CL> struct ResidentGeneric : Resid
                 partner_fields<R, uint16_t, CUB, QUA>(tb, S.cf, cv, d, b, hb, hc, hq);
                 const V3<R> hext = vsub(vadd(vadd(hb, hc), hq), V3<R>{S.cf.h[3 * b], S.cf.h[3 * b + 1], S.cf.h[3 * b + 2]});
                 const V3<R> s = sp.get(d);
-                const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
+                const Draw<R> dr(dg, msweep, this->key, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
                 const R dE = delta_e<R>(S.cf, b, s, sn, hext);
                 bool accept = dE < R(0);
-                if (!accept) accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
+                if (!accept) accept = dr.acc(dg, msweep, this->key, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
                 if (accept) {
                     sp.set(d, sn);
                     acc++;
@@ -471,8 +460,11 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     static constexpr int kCoefSmem = CSMC_MAX_COLOURS * kClassBlock + (BIL ? CSMC_MAX_COLOURS * WMAX * 9 : 0);
     static constexpr int OFF_A = WMAX, OFF_Q = WMAX + 9, OFF_E2 = WMAX + 18, OFF_H = WMAX + 27;
     static constexpr bool kPartnerWords = true;
+    // a Metropolis sweep can also sum the energy and |M| of its final state
+    // (two colour classes: every bond joins them)
+    static constexpr bool kMeasuringSweep = true;
     using B = ResidentCommon<R, CL>;
-    using B::c;
+    using B::key;
     using B::rank;
     using B::S;
     using B::scoef;
@@ -482,9 +474,9 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
     uint32_t rb[CL]; // shared::cluster address of local site 0 of rank (rank + q) % CL, by q (CL > 1)
     uint32_t comp;   // double precision: bytes between the x, y and z blocks
 
-    __device__ ResidentFast(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, int c_, int slot_, int rk, R *coef,
-                            const uint4 *pv_, bool pv_shared)
-        : B{s, sp_, sy_, c_, slot_, rk, coef}, pv(pv_) {
+    __device__ ResidentFast(const ResSys<R> &s, Spins<R> sp_, Sync<CL> sy_, uint32_t key_, int slot_, int rk,
+                            R *coef, const uint4 *pv_, bool pv_shared)
+        : B{s, sp_, sy_, key_, slot_, rk, coef}, pv(pv_) {
         pvs = pv_shared ? smem_u32(pv_) : 0u;
         comp = (uint32_t)(S.Npl * sizeof(double));
         if (CL > 1) {
@@ -621,12 +613,23 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         }
     }
 
-    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep) const {
+    // One Metropolis sweep.  MEASURE (lattices of two colour classes): each
+    // site's final spin s also adds to this thread's partials meas[0..3] =
+    // {energy, M_x, M_y, M_z}: s.(O + P/2).s - s.h for every site, plus s.hb
+    // (its whole bilinear field) for the sites of class 1 -- their partners
+    // are all of class 0 and already final, and every bond, having one end in
+    // each class, is counted once; the sum is total_energy
+    // (hamiltonian.jl:70-132) of the state the sweep leaves.
+    template <bool MEASURE = false>
+    __device__ unsigned metro_sweep(int kind, R sigma, R invT, double T, uint32_t msweep, R *meas = nullptr) const {
         unsigned acc = 0;
+        R pe = R(0), pmx = R(0), pmy = R(0), pmz = R(0);
         for (int col = 0; col < S.n_colours; col++) {
-            R J[W], q[9];
+            R J[W], q[9], e2[9];
             V3<R> h;
             load_coef(col, OFF_Q, J, q, h);
+            if (MEASURE) load_coef(col, OFF_E2, J, e2, h);
+            const bool bonds = MEASURE && col == 1;
             const int st = this->col_begin(col), n = this->col_size(col);
             uint4 wn = first_word(st, n);
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -637,18 +640,33 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 const V3<R> hb = gather(col, J, w);
                 const V3<R> s = sp.get(d);
                 const V3<R> hext = vsub(hb, h);
-                const Draw<R> dr(dg, msweep, (uint32_t)c, S.k0, S.k1);
+                const Draw<R> dr(dg, msweep, this->key, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
                 using F = Fp<R>;
                 const R dE = F::add(F::sub(dot(sn, onsite(q, sn)), dot(s, onsite(q, s))), dot(vsub(sn, s), hext));
                 bool accept = dE < R(0);
-                if (!accept) accept = dr.acc(dg, msweep, (uint32_t)c, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
+                if (!accept) accept = dr.acc(dg, msweep, this->key, S.k0, S.k1) < Math<R>::exp_(boltz_arg(dE, invT, T));
                 if (accept) {
                     sp.set(d, sn);
                     acc++;
                 }
+                if (MEASURE) {
+                    const V3<R> f = accept ? sn : s;
+                    R part = F::sub(dot(f, onsite(e2, f)), dot(f, h));
+                    if (bonds) part = F::add(part, dot(f, hb));
+                    pe = F::add(pe, part);
+                    pmx = F::add(pmx, f.x);
+                    pmy = F::add(pmy, f.y);
+                    pmz = F::add(pmz, f.z);
+                }
             }
             this->sy.bar();
+        }
+        if (MEASURE) {
+            meas[0] = pe;
+            meas[1] = pmx;
+            meas[2] = pmy;
+            meas[3] = pmz;
         }
         return acc;
     }
@@ -692,8 +710,8 @@ __global__ void __launch_bounds__(NT, 1)
                ChainState cs, RunDesc rd) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t bar;
-    __shared__ double scratch[32];
-    __shared__ double red[3];
+    __shared__ double scratch[4 * 32];
+    __shared__ double red[4];
     __shared__ int s_item;
     __shared__ int s_ok;
     __shared__ uint32_t s_vote;
@@ -701,20 +719,16 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ R s_invT;
     __shared__ ResSys<R> s_sys;
     __shared__ R s_coef[K::kCoefSmem];
-    __shared__ uint64_t pbar;
-    __shared__ uint32_t pphase;
     uint32_t parity = 0;
     const int rank = CL == 1 ? 0 : (int)cluster_ctarank();
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
-        mbar_init(&pbar, CL);
-        pphase = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (CL > 1) cluster_sync_all(); // every rank's phase barrier exists before any remote arrive
+    if (CL > 1) cluster_sync_all(); // every rank has started before any reads another's shared memory
     const int64_t dosweep = rd.or_rate == 0 ? 1 : rd.or_rate;
-    const Sync<CL> sync{scratch, red, &pbar, &pphase, cs.error_flag};
+    const Sync<CL> sync{scratch, red, cs.error_flag};
     int item = CL == 1 ? 0 : (int)cluster_index();
 
     for (;; item += (CL == 1 ? 0 : (int)cluster_count())) {
@@ -796,7 +810,7 @@ __global__ void __launch_bounds__(NT, 1)
             cluster_sync_all();
         }
 
-        const K k(S, sp, sync, c, 0, rank, s_coef, words ? swords : gwords, words);
+        const K k(S, sp, sync, __ldg(cs.chain_id + c), 0, rank, s_coef, words ? swords : gwords, words);
         k.prepare();
         const bool writer = threadIdx.x == 0 && rank == 0;
         double E = cs.E_chain[c];
@@ -838,8 +852,20 @@ __global__ void __launch_bounds__(NT, 1)
                     sweeps++;
                 }
                 const bool metro = it % dosweep == 0;
+                bool have_M = false; // |M| of this iteration's state summed by its Metropolis sweep
+                double M = 0.0;
                 if (metro) {
-                    const unsigned a = k.metro_sweep(rd.kind, (R)s_sigma, invT, T, msweep);
+                    // energy needed: exchange point, a probe before the next
+                    // Metropolis sweep, or the last Metropolis sweep of the window
+                    bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
+                    for (int64_t q = it; q < it + dosweep && q < w1 && !needE; q++) needE = is_probe(rd, q);
+                    needE = needE || it + dosweep >= w1;
+                    // with two colour classes the sweep itself sums the energy
+                    // and |M| of the state it leaves
+                    const bool measure = K::kMeasuringSweep && needE && S.n_colours == 2;
+                    R meas[4];
+                    const unsigned a = measure ? k.template metro_sweep<true>(rd.kind, (R)s_sigma, invT, T, msweep, meas)
+                                               : k.template metro_sweep<false>(rd.kind, (R)s_sigma, invT, T, msweep);
                     msweep++;
                     sweeps++;
                     const double at = sync.sum(a); // exact: an integer sum per warp
@@ -853,12 +879,13 @@ __global__ void __launch_bounds__(NT, 1)
                         }
                     }
                     __syncthreads();
-                    // energy needed: exchange point, a probe before the next
-                    // Metropolis sweep, or the last Metropolis sweep of the window
-                    bool needE = rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
-                    for (int64_t q = it; q < it + dosweep && q < w1 && !needE; q++) needE = is_probe(rd, q);
-                    needE = needE || it + dosweep >= w1;
-                    if (needE) {
+                    if (measure) {
+                        double o[4];
+                        sync.sum4(meas[0], meas[1], meas[2], meas[3], o);
+                        if (threadIdx.x == 0) E = o[0];
+                        M = sqrt(o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+                        have_M = true;
+                    } else if (needE) {
                         const double e = k.energy();
                         if (threadIdx.x == 0) E = e;
                     }
@@ -867,7 +894,7 @@ __global__ void __launch_bounds__(NT, 1)
                 // recorded after the exchange, from M_chain
                 const bool swap_here = metro && rd.swap_enabled && rd.swap_rate > 0 && it % rd.swap_rate == 0;
                 if (is_probe(rd, it)) {
-                    const double M = k.magnetization();
+                    if (!have_M) M = k.magnetization();
                     if (writer) {
                         const int64_t kq = (it - rd.probe_first) / rd.probe_rate;
                         if (!swap_here && kq >= 0 && kq < rd.probe_cap) {

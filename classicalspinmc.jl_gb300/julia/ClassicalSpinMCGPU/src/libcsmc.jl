@@ -168,6 +168,8 @@ c_get_spins_all(ctx, spins::Array{Float64}) =
 c_random_spins(ctx, seed::Integer) =
     check(ccall((:csmc_random_spins, libcsmc), Cint, (Ptr{Cvoid}, UInt64), ctx, UInt64(seed)))
 
+c_set_chain_ids(ctx, ids::Vector{UInt32}) =
+    check(ccall((:csmc_set_chain_ids, libcsmc), Cint, (Ptr{Cvoid}, Ptr{UInt32}), ctx, ids))
 c_set_temperatures(ctx, T::Vector{Float64}) =
     check(ccall((:csmc_set_temperatures, libcsmc), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx, T))
 c_set_sigma(ctx, sigma::Vector{Float64}) =

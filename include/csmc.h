@@ -194,6 +194,14 @@ int csmc_get_spins_all(void *ctx, double *spins);
  * (Lattice initialCondition=:random, lattice.jl:76-79). */
 int csmc_random_spins(void *ctx, uint64_t seed);
 
+/* The key of each replica's random streams (Philox counter word 2), one per
+ * replica in creation order (replica k starts in slot k and keeps its key
+ * when exchanges move it).  Default: k.  A replica given the same key, seed
+ * and spins in another context -- alone, or in a different batch -- draws
+ * the same numbers and so runs the same chain.  Affects later sweeps and
+ * csmc_random_spins.  No counterpart in the reference (its ranks draw from
+ * unseeded task-local generators). */
+int csmc_set_chain_ids(void *ctx, const uint32_t *ids);
 /* mc.T per slot (monte_carlo.jl:72); also resets the slot permutation. */
 int csmc_set_temperatures(void *ctx, const double *T);
 /* mc.sigma per slot (monte_carlo.jl:79, metropolis.jl:84-87). */

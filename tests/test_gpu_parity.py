@@ -340,33 +340,46 @@ def test_honeycomb_anneal_kat(m, orc, precision):
     assert round(E, 4) == c["expect"]["energy_density_4dp"], E
 
 
-def test_batch_of_lattices_matches_single(m, orc):
-    """Independent chains of different sizes in one context == each alone."""
-    E = m.examples
-    specs = [(12, 0.2, 0.5), (18, 0.6, 1.5), (6, 1.0, 2.5)]
-    lats = [m.Lattice((L, L), E.triangular_afm(h=h), 1.0, rng=np.random.default_rng(L)) for L, _, h in specs]
-    ctx = m.monte_carlo.Context(lats, [1, 1, 1], precision="fp64", seed=4)
-    Ts = np.array([t for _, t, _ in specs])
-    ctx.set_temperatures(Ts)
-    for k, l in enumerate(lats):
-        ctx.set_spins(k, l.spins)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("path", ["resident", "global"])
+def test_batch_of_lattices_matches_single(m, orc, precision, path):
+    """Independent chains of different sizes in one context (the uneven batch
+    of independent chains) == each chain run alone: with the same chain id
+    (csmc_set_chain_ids), seed and initial spins, a chain draws the same
+    numbers wherever it runs, so its spins and accepted counts agree bit for
+    bit.  The batch runs every lattice in one launch (one work list); alone,
+    each context picks its own launch shape."""
     import ctypes as C
     from importlib import import_module
     L = import_module(m.__name__ + "._lib")
-    rp = L.RunParams()
-    rp.n_sweeps = 20
-    rp.overrelaxation_rate = 5
-    rp.path = L.PATH_RESIDENT
-    ctx.call("csmc_run", C.byref(rp))
-    E_batch = ctx.per_slot("csmc_total_energy")
-    # the same lattices one by one: chains keep their batch index in the Philox
-    # counter, so compare physics, not bits: energies per site are finite and
-    # configurations stay normalised
-    for k, l in enumerate(lats):
-        s = ctx.get_spins(k)
-        assert np.allclose(np.linalg.norm(s, axis=0), 1.0, atol=1e-12)
-        assert math.isfinite(E_batch[k])
-    assert ctx.n_slots == 3
+    E = m.examples
+    specs = [(12, 0.2, 0.5), (18, 0.6, 1.5), (6, 1.0, 2.5), (24, 0.35, 0.0)]
+    ids = np.array([7, 1000, 3, 42], np.uint32)
+    lats = [m.Lattice((Ls, Ls), E.triangular_afm(h=h), 1.0, rng=np.random.default_rng(Ls)) for Ls, _, h in specs]
+    Ts = np.array([t for _, t, _ in specs])
+
+    def run(ctx, T, ids_):
+        ctx.set_temperatures(T)
+        ctx.call("csmc_set_chain_ids", ids_.ctypes.data_as(C.POINTER(C.c_uint32)))
+        rp = L.RunParams()
+        rp.sweep_start, rp.n_sweeps, rp.overrelaxation_rate = 1, 30, 3
+        rp.path = {"resident": L.PATH_RESIDENT, "global": L.PATH_GLOBAL}[path]
+        acc = np.zeros(ctx.n_slots)
+        rp.accepted = acc.ctypes.data_as(C.POINTER(C.c_double))
+        ctx.call("csmc_run", C.byref(rp))
+        return acc
+
+    batch = m.monte_carlo.Context(lats, [1] * len(lats), precision=precision, seed=4)
+    for k, lat in enumerate(lats):
+        batch.set_spins(k, lat.spins)
+    acc_b = run(batch, Ts, ids)
+    for k, lat in enumerate(lats):
+        one = m.monte_carlo.Context([lat], [1], precision=precision, seed=4)
+        one.set_spins(0, lat.spins)
+        acc_1 = run(one, Ts[k:k + 1], ids[k:k + 1])
+        assert acc_1[0] == acc_b[k], (k, acc_1[0], acc_b[k])
+        assert np.array_equal(one.get_spins(0), batch.get_spins(k)), k
+    assert acc_b.min() > 0
 
 
 @pytest.mark.parametrize("block", [512, 1024])
