@@ -121,6 +121,8 @@ SIGNATURES = {
                               f64p]),
     "csmc_set_cluster_size": (C.c_int, [_vp, C.c_int32]),
     "csmc_cluster_size": (C.c_int, [_vp, i32p]),
+    "csmc_set_size_groups": (C.c_int, [_vp, C.c_int32]),
+    "csmc_size_groups": (C.c_int, [_vp, i32p]),
     "csmc_autotune": (C.c_int, [_vp, C.POINTER(RunParams), C.c_int32, C.POINTER(TuneEntry), C.c_int32, i32p]),
     "csmc_structure_factor": (C.c_int, [_vp, C.c_int32, C.c_int32, f64p, C.c_int64, f64p, f64p]),
     "csmc_selftest_timeout": (C.c_int, [_vp, C.c_int32]),

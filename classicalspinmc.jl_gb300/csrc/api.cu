@@ -107,6 +107,29 @@ struct System {
     DevBuf<double> cw, cw_ref;
 };
 
+// Lattices that share one resident launch: its CTAs per replica (cluster
+// size), threads per CTA, shared-memory size and work list.  A context is one
+// group, or -- size groups, for batches of lattices of very different sizes --
+// one group per band of replica sizes, whose launches run side by side on
+// streams of their own (small replicas in small CTAs, several per SM; the
+// largest split over clusters).
+struct Group {
+    std::vector<int> sys; // lattices (indices into Ctx::sys)
+    int cl = 1;           // CTAs per replica
+    int n_items = 0;      // replicas of the group
+    DevBuf<int2> items;   // {lattice, replica}, largest replicas first
+    DevBuf<int> work_ctr;
+    cudaStream_t st = nullptr; // own stream (size groups only)
+    cudaEvent_t done = nullptr;
+    Group() = default;
+    Group(const Group &) = delete;
+    Group &operator=(const Group &) = delete;
+    ~Group() {
+        if (done) cudaEventDestroy(done);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
 struct Ctx {
     int precision = CSMC_FP64;
     uint64_t seed = 0;
@@ -122,17 +145,21 @@ struct Ctx {
     DevBuf<uint32_t> chain_id;           // per chain: the key of its Philox streams
     DevBuf<unsigned long long> sweep_acc;
     DevBuf<unsigned int> drift_bits;
-    DevBuf<int> error_flag, work_ctr;
+    DevBuf<int> error_flag;
     DevBuf<unsigned int> grid_bar; // arrival counter of the persistent kernel's grid barrier
     bool persistent_ok = true;     // cleared if a cooperative launch is refused
     bool persistent_on = true;     // csmc_set_persistent
     DevBuf<double> part, stage, rec_E, rec_M;
     DevBuf<ResSys<float>> fres;
     DevBuf<ResSys<double>> dres;
-    DevBuf<int2> items;
     DevBuf<int2> lattices; // per lattice {first slot, replicas} (exchange kernel)
-    int n_items = 0;
-    int cl = 1;         // CTAs per replica of the resident kernel
+    int n_items = 0;       // replicas of every lattice
+    std::vector<std::unique_ptr<Group>> groups; // one, or the size groups
+    bool size_groups = false;                   // csmc_set_size_groups / the autotuner's choice
+    int group_block_cap = 0; // size groups: at most this many threads per CTA (0: none), so CTAs of
+                             // several groups share an SM (the autotuner's choice)
+    cudaEvent_t fork = nullptr;                 // size groups start after the work queued before them
+    int cl = 1;         // CTAs per replica of the resident kernel (one group; 0 with size groups)
     int block_pref = 0; // threads per CTA chosen by csmc_autotune (0: automatic)
     bool global_pref = false; // csmc_autotune found the global path faster for CSMC_PATH_AUTO runs
     DevBuf<double> lambda_slot; // mc.lambda per slot (constrained kinds)
@@ -160,6 +187,8 @@ struct Ctx {
             cudaEventDestroy(e.first);
             cudaEventDestroy(e.second);
         }
+        groups.clear(); // their streams before the context's
+        if (fork) cudaEventDestroy(fork);
         if (run_e0) cudaEventDestroy(run_e0);
         if (run_e1) cudaEventDestroy(run_e1);
         if (h_flag) cudaFreeHost(h_flag);
@@ -423,113 +452,179 @@ static int64_t spin_bytes(const Ctx &C, int64_t n) { return C.precision == CSMC_
 // reserve for the kernel's static shared memory (at most about 6 KB).
 static int64_t dynamic_smem_limit(const Ctx &C) { return (int64_t)C.max_smem - 8 * 1024; }
 
-// Cluster size of the resident kernel for a context: the largest of 2 and 4
-// whose clusters all fit on the device at once with at least 1024 sites per
-// rank, else 1; a larger size when a replica fits shared memory only split.
-// `requested` = 0 picks automatically; 1, 2 or 4 forces that size (if the
-// specialised kernel applies and the parts fit shared memory).
-static void choose_cluster(Ctx &C, int requested) {
+// Does a cluster size of c CTAs per replica fit the lattices `idx` (n_items
+// replicas)?  Parts of at most 16383 sites (14-bit owner-local indices) that
+// fit shared memory; `prefer`: also at least 1024 sites per rank and all
+// clusters of the group on the device at once.
+static bool cluster_fits(const Ctx &C, const std::vector<int> &idx, int n_items, int c, bool prefer) {
     const int64_t limit = dynamic_smem_limit(C);
-    auto fits = [&](int c, bool prefer) {
-        if (c == 1) {
-            for (auto &S : C.sys)
-                if (S->plan.Np > 65536 || spin_bytes(C, S->plan.Np) > limit) return false;
-            return true;
-        }
-        for (auto &S : C.sys) {
-            const int64_t per_rank = (S->plan.Np + c - 1) / c + 32 * (S->plan.n_colours + 1);
-            if (per_rank > 16384 || spin_bytes(C, per_rank) > limit) return false;
-            if (prefer && S->plan.N / c < 1024) return false;
-        }
-        return !prefer || (int64_t)C.n_items * c <= C.n_sms;
-    };
-    int best = 1;
+    if (c == 1) {
+        for (int k : idx)
+            if (C.sys[k]->plan.Np > 65536 || spin_bytes(C, C.sys[k]->plan.Np) > limit) return false;
+        return true;
+    }
+    for (int k : idx) {
+        const Plan &P = C.sys[k]->plan;
+        const int64_t per_rank = (P.Np + c - 1) / c + 32 * (P.n_colours + 1);
+        if (per_rank > 16384 || spin_bytes(C, per_rank) > limit) return false;
+        if (prefer && P.N / c < 1024) return false;
+    }
+    return !prefer || (int64_t)n_items * c <= C.n_sms;
+}
+
+// Cluster size of a group: the largest of 2 and 4 whose clusters all fit on
+// the device at once with at least 1024 sites per rank, else 1; a larger size
+// when a replica fits shared memory only split.  `requested` = 0 picks
+// automatically; 1, 2 or 4 forces that size (if the parts fit shared memory).
+static int pick_cluster(const Ctx &C, const std::vector<int> &idx, int n_items, int requested) {
     if (requested > 0) {
         require(requested == 1 || requested == 2 || requested == 4, CSMC_ERR_INVALID, "cluster size must be 1, 2 or 4");
-        require(requested == 1 || fits(requested, false), CSMC_ERR_UNSUPPORTED,
+        require(requested == 1 || cluster_fits(C, idx, n_items, requested, false), CSMC_ERR_UNSUPPORTED,
                 "this cluster size needs parts of at most 16383 sites that fit shared memory");
-        best = requested;
-    } else {
-        int pick = 0;
-        for (int c : {1, 2, 4})
-            if (fits(c, true)) pick = c;
-        if (!pick) // no preferred size: the smallest one that fits
-            for (int c : {1, 2, 4})
-                if (fits(c, false)) {
-                    pick = c;
-                    break;
-                }
-        best = pick ? pick : 1;
+        return requested;
     }
-    C.cl = best;
-    for (auto &Sp : C.sys) {
-        System &S = *Sp;
-        if (best > 1) {
-            S.cl_layout = make_cluster_layout(S.plan, best);
-            S.q2c.upload(S.cl_layout.q2);
-            S.q3c.upload(S.cl_layout.q3);
-            S.q4c.upload(S.cl_layout.q4);
-            S.patc.upload(S.cl_layout.pat);
-            if (S.fast_ok) {
-                const ClusterLayout &L = S.cl_layout;
-                const int W = std::max(S.plan.W2, 1);
-                std::vector<uint4> all;
-                for (int k = 0; k < L.ranks; k++) {
-                    std::vector<uint16_t> part(L.q2.begin() + (size_t)k * W * L.Npl,
-                                               L.q2.begin() + (size_t)(k + 1) * W * L.Npl);
-                    const uint32_t sent = (uint32_t)(L.Npl - 32);
-                    std::vector<uint4> pk = pack8(part, S.plan.W2, L.Npl, [&](int64_t) { return sent; });
-                    all.insert(all.end(), pk.begin(), pk.end());
-                }
-                S.q2v.upload(all);
+    int pick = 0;
+    for (int c : {1, 2, 4})
+        if (cluster_fits(C, idx, n_items, c, true)) pick = c;
+    if (!pick) // no preferred size: the smallest one that fits
+        for (int c : {1, 2, 4})
+            if (cluster_fits(C, idx, n_items, c, false)) {
+                pick = c;
+                break;
             }
-            S.resident_smem = (size_t)spin_bytes(C, S.cl_layout.Npl);
-            S.resident_ok = (int64_t)S.resident_smem <= limit && S.plan.n_colours <= CSMC_MAX_COLOURS;
-        } else {
-            S.cl_layout = ClusterLayout();
-            S.resident_smem = (size_t)spin_bytes(C, S.plan.Np);
-            S.resident_ok = S.plan.Np <= 65536 && (int64_t)S.resident_smem <= limit &&
-                            S.plan.n_colours <= CSMC_MAX_COLOURS;
+    return pick ? pick : 1;
+}
+
+// Lay a lattice out for clusters of `cl` CTAs per replica (cl = 1: one CTA).
+static void layout_for_cluster(Ctx &C, System &S, int cl) {
+    const int64_t limit = dynamic_smem_limit(C);
+    if (cl > 1) {
+        S.cl_layout = make_cluster_layout(S.plan, cl);
+        S.q2c.upload(S.cl_layout.q2);
+        S.q3c.upload(S.cl_layout.q3);
+        S.q4c.upload(S.cl_layout.q4);
+        S.patc.upload(S.cl_layout.pat);
+        if (S.fast_ok) {
+            const ClusterLayout &L = S.cl_layout;
+            const int W = std::max(S.plan.W2, 1);
+            std::vector<uint4> all;
+            for (int k = 0; k < L.ranks; k++) {
+                std::vector<uint16_t> part(L.q2.begin() + (size_t)k * W * L.Npl,
+                                           L.q2.begin() + (size_t)(k + 1) * W * L.Npl);
+                const uint32_t sent = (uint32_t)(L.Npl - 32);
+                std::vector<uint4> pk = pack8(part, S.plan.W2, L.Npl, [&](int64_t) { return sent; });
+                all.insert(all.end(), pk.begin(), pk.end());
+            }
+            S.q2v.upload(all);
         }
+        S.resident_smem = (size_t)spin_bytes(C, S.cl_layout.Npl);
+        S.resident_ok = (int64_t)S.resident_smem <= limit && S.plan.n_colours <= CSMC_MAX_COLOURS;
+    } else {
+        S.cl_layout = ClusterLayout();
+        S.resident_smem = (size_t)spin_bytes(C, S.plan.Np);
+        S.resident_ok =
+            S.plan.Np <= 65536 && (int64_t)S.resident_smem <= limit && S.plan.n_colours <= CSMC_MAX_COLOURS;
     }
 }
 
-static ResidentSel resident_selection(const Ctx &C);
+static int group_items(const Ctx &C, const std::vector<int> &idx) {
+    int n = 0;
+    for (int k : idx) n += C.sys[k]->R;
+    return n;
+}
 
-// Resident descriptors of every lattice and the work list (largest replicas
-// first).  The specialised kernel also stages each CTA's packed partner
-// words in shared memory when they fit beside the spins of every lattice.
-static void upload_resident(Ctx &C) {
-    const ResidentSel sel = resident_selection(C);
-    const int stat = !sel.fast ? -1
-                     : C.precision == CSMC_FP32 ? resident_static_smem<float>(sel)
-                                                : resident_static_smem<double>(sel);
-    bool stage = sel.fast && stat >= 0;
-    for (auto &S : C.sys) {
-        const int64_t nl = C.cl > 1 ? S->cl_layout.Npl : S->plan.Np;
-        const int64_t spins = (spin_bytes(C, nl) + 15) / 16 * 16;
-        stage = stage && spins + 16 * nl + stat <= (int64_t)C.max_smem;
+// One group of every lattice with the cluster size `requested` (0: automatic).
+static void choose_cluster(Ctx &C, int requested) {
+    std::vector<int> all(C.sys.size());
+    std::iota(all.begin(), all.end(), 0);
+    const int cl = pick_cluster(C, all, C.n_items, requested);
+    for (auto &S : C.sys) layout_for_cluster(C, *S, cl);
+    C.groups.clear();
+    C.groups.push_back(std::make_unique<Group>());
+    C.groups[0]->sys = all;
+    C.groups[0]->cl = cl;
+    C.groups[0]->n_items = C.n_items;
+    C.cl = cl;
+    C.size_groups = false;
+}
+
+// Size groups: lattices sorted by size, a new group wherever the padded size
+// drops below half of the group's largest; each group picks its own cluster
+// size (or, clusters = false, one CTA per replica).  Fewer than two groups:
+// one group (choose_cluster).  Returns whether size groups are in use.
+static bool make_size_groups(Ctx &C, bool clusters = true) {
+    std::vector<int> order(C.sys.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return C.sys[a]->plan.Np > C.sys[b]->plan.Np; });
+    std::vector<std::vector<int>> bands;
+    for (int k : order) {
+        if (bands.empty() || 2 * C.sys[k]->plan.Np < C.sys[bands.back()[0]]->plan.Np) bands.emplace_back();
+        bands.back().push_back(k);
     }
-    for (auto &S : C.sys) {
-        const int64_t nl = C.cl > 1 ? S->cl_layout.Npl : S->plan.Np;
-        S->pv_stage = stage;
-        S->resident_smem = (size_t)(stage ? (spin_bytes(C, nl) + 15) / 16 * 16 + 16 * nl : spin_bytes(C, nl));
+    if (bands.size() < 2) {
+        choose_cluster(C, 0);
+        return false;
+    }
+    C.groups.clear();
+    for (auto &band : bands) {
+        auto G = std::make_unique<Group>();
+        G->sys = band;
+        G->n_items = group_items(C, band);
+        G->cl = clusters ? pick_cluster(C, band, G->n_items, 0) : 1;
+        for (int k : band) layout_for_cluster(C, *C.sys[k], G->cl);
+        CK(cudaStreamCreateWithFlags(&G->st, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&G->done, cudaEventDisableTiming));
+        G->work_ctr.alloc(1);
+        C.groups.push_back(std::move(G));
+    }
+    if (!C.fork) CK(cudaEventCreateWithFlags(&C.fork, cudaEventDisableTiming));
+    C.cl = 0;
+    C.size_groups = true;
+    return true;
+}
+
+static ResidentSel resident_selection(const Ctx &C, const Group &G);
+
+// Resident descriptors of every lattice and the work list of each group
+// (largest replicas first).  The specialised kernel also stages each CTA's
+// packed partner words in shared memory when they fit beside the spins of
+// every lattice of the group.
+static void upload_resident(Ctx &C) {
+    for (auto &Gp : C.groups) {
+        Group &G = *Gp;
+        const ResidentSel sel = resident_selection(C, G);
+        const int stat = !sel.fast ? -1
+                         : C.precision == CSMC_FP32 ? resident_static_smem<float>(sel)
+                                                    : resident_static_smem<double>(sel);
+        bool stage = sel.fast && stat >= 0;
+        for (int k : G.sys) {
+            const System &S = *C.sys[k];
+            const int64_t nl = G.cl > 1 ? S.cl_layout.Npl : S.plan.Np;
+            const int64_t spins = (spin_bytes(C, nl) + 15) / 16 * 16;
+            stage = stage && spins + 16 * nl + stat <= (int64_t)C.max_smem;
+        }
+        std::vector<int2> items;
+        for (int k : G.sys) {
+            System &S = *C.sys[k];
+            const int64_t nl = G.cl > 1 ? S.cl_layout.Npl : S.plan.Np;
+            S.pv_stage = stage;
+            S.resident_smem = (size_t)(stage ? (spin_bytes(C, nl) + 15) / 16 * 16 + 16 * nl : spin_bytes(C, nl));
+            for (int r = 0; r < S.R; r++) items.push_back(make_int2(k, r));
+        }
+        std::stable_sort(items.begin(), items.end(),
+                         [&](int2 a, int2 b) { return C.sys[a.x]->plan.Np > C.sys[b.x]->plan.Np; });
+        G.items.upload(items);
+        G.n_items = (int)items.size();
+        if (!G.work_ctr.n) G.work_ctr.alloc(1);
     }
     std::vector<ResSys<float>> fr;
     std::vector<ResSys<double>> dr;
-    std::vector<int2> items;
-    for (size_t k = 0; k < C.sys.size(); k++) {
-        System &S = *C.sys[k];
-        if (C.precision == CSMC_FP32) fr.push_back(make_res(S, S.fa));
-        else dr.push_back(make_res(S, S.da));
-        for (int r = 0; r < S.R; r++) items.push_back(make_int2((int)k, r));
+    for (auto &Sp : C.sys) {
+        if (C.precision == CSMC_FP32) fr.push_back(make_res(*Sp, Sp->fa));
+        else dr.push_back(make_res(*Sp, Sp->da));
     }
-    std::stable_sort(items.begin(), items.end(),
-                     [&](int2 a, int2 b) { return C.sys[a.x]->plan.Np > C.sys[b.x]->plan.Np; });
     if (C.precision == CSMC_FP32) C.fres.upload(fr);
     else C.dres.upload(dr);
-    C.items.upload(items);
-    C.n_items = (int)items.size();
 }
 
 // (float)(1 / T[k]): the reciprocal temperatures the single-precision sweeps
@@ -602,7 +697,6 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     C->drift_bits.upload(&zb, 1);
     int zi = 0;
     C->error_flag.upload(&zi, 1);
-    C->work_ctr.upload(&zi, 1);
     unsigned int zu = 0;
     C->grid_bar.upload(&zu, 1);
     size_t part = 0, stage = 0;
@@ -697,13 +791,18 @@ static const double *device_view(const void *host) {
 }
 
 // Slots [first, first+n) of one lattice from / to the FP64 reference layout:
-// one conversion launch, reading or writing pinned host memory directly when
-// the caller's buffer is pinned, else through the device staging buffer.
-// Returns after the host buffer has been read (set) or written (get).
+// one bulk copy between the host buffer and the device staging buffer and one
+// conversion launch.  A small pinned buffer (below kDirectBytes) is read or
+// written by the conversion kernel in place instead: one launch, no copy; a
+// large one moves faster as one bulk copy (the kernel's scattered accesses
+// would cross the host link element by element).  Returns after the host
+// buffer has been read (set) or written (get).
+constexpr size_t kDirectBytes = (size_t)1 << 20;
+
 static void set_spins_range(Ctx &C, System &S, int first, int n, const double *host) {
     if (n <= 0) return;
     const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
-    const double *src = device_view(host);
+    const double *src = bytes < kDirectBytes ? device_view(host) : nullptr;
     if (!src) {
         CK(cudaMemcpyAsync(C.stage.p, host, bytes, cudaMemcpyHostToDevice, C.st));
         src = C.stage.p;
@@ -715,7 +814,7 @@ static void set_spins_range(Ctx &C, System &S, int first, int n, const double *h
 static void get_spins_range(Ctx &C, System &S, int first, int n, double *host) {
     if (n <= 0) return;
     const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
-    double *dst = const_cast<double *>(device_view(host));
+    double *dst = bytes < kDirectBytes ? const_cast<double *>(device_view(host)) : nullptr;
     const bool direct = dst != nullptr;
     if (!direct) dst = C.stage.p;
     with_args(C, S, [&](auto &a) { launch_gather(a, C.chain_of.p, first, n, dst, C.st); });
@@ -866,27 +965,30 @@ static int choose_path(Ctx &C, int requested, int kind) {
     return all && !C.global_pref ? CSMC_PATH_RESIDENT : CSMC_PATH_GLOBAL;
 }
 
-// Threads per CTA of the resident kernel.  `hint` (a multiple of 32) forces a
-// size, capped at the kernel's maximum (1024 for the specialised kernel with
-// scalar couplings and at most diagonal onsite terms, else 512).  Otherwise
-// the specialised kernel gets the smallest multiple of 32 that gives every
-// thread the same number of sites of the largest colour-class part between
-// two barriers, and the generic kernel its maximum.
-static int resident_block(Ctx &C, int hint) {
-    const ResidentSel sel = resident_selection(C);
-    const int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
-    if (hint == 0 && C.block_pref > 0) hint = C.block_pref;
+// Threads per CTA of a group's resident kernel.  `hint` (a multiple of 32)
+// forces a size, capped at the kernel's maximum (896 for the specialised
+// kernel with scalar couplings and at most diagonal onsite terms, else 512).
+// Otherwise the specialised kernel gets the smallest multiple of 32 that gives
+// every thread the same number of sites of the largest colour-class part
+// between two barriers, and the generic kernel its maximum.  The autotuner's
+// block applies to a context of one group.
+static int resident_block(Ctx &C, const Group &G, int hint) {
+    const ResidentSel sel = resident_selection(C, G);
+    int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
+    if (C.size_groups && C.group_block_cap >= 32) mx = std::min(mx, C.group_block_cap);
+    if (hint == 0 && C.block_pref > 0 && !C.size_groups) hint = C.block_pref;
     if (hint > 0) {
         require(hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
         return std::min(hint, mx);
     }
     if (!sel.fast) return mx;
     int64_t n = 32;
-    for (auto &S : C.sys) {
-        const Plan &P = S->plan;
+    for (int k : G.sys) {
+        const System &S = *C.sys[k];
+        const Plan &P = S.plan;
         for (int col = 0; col < P.n_colours; col++) {
-            if (C.cl > 1)
-                for (int k = 0; k < C.cl; k++) n = std::max(n, S->cl_layout.loc_count[(size_t)k * P.n_colours + col]);
+            if (G.cl > 1)
+                for (int q = 0; q < G.cl; q++) n = std::max(n, S.cl_layout.loc_count[(size_t)q * P.n_colours + col]);
             else
                 n = std::max(n, P.col_count[col]);
         }
@@ -895,27 +997,28 @@ static int resident_block(Ctx &C, int hint) {
     return (int)std::min<int64_t>(mx, (n + 32 * iters - 1) / (32 * iters) * 32);
 }
 
-// The resident kernel for every lattice of the context: the specialised one
-// when all lattices allow it (with the widest coupling classes among them),
-// else the generic one.
-static ResidentSel resident_selection(const Ctx &C) {
-    ResidentSel sel{true, 0, 0, 4, false, false, C.cl};
-    for (auto &S : C.sys) {
-        sel.fast = sel.fast && S->fast_ok;
-        sel.bil = std::max(sel.bil, S->bil_class);
-        sel.ons = std::max(sel.ons, S->ons_class);
-        sel.width = std::max(sel.width, S->plan.W2 <= 4 ? 4 : S->plan.W2 <= 6 ? 6 : 8);
-        sel.cub = sel.cub || S->cub;
-        sel.qua = sel.qua || S->qua;
+// The resident kernel for the lattices of a group: the specialised one when
+// all of them allow it (with the widest coupling classes among them), else
+// the generic one.
+static ResidentSel resident_selection(const Ctx &C, const Group &G) {
+    ResidentSel sel{true, 0, 0, 4, false, false, G.cl};
+    for (int k : G.sys) {
+        const System &S = *C.sys[k];
+        sel.fast = sel.fast && S.fast_ok;
+        sel.bil = std::max(sel.bil, S.bil_class);
+        sel.ons = std::max(sel.ons, S.ons_class);
+        sel.width = std::max(sel.width, S.plan.W2 <= 4 ? 4 : S.plan.W2 <= 6 ? 6 : 8);
+        sel.cub = sel.cub || S.cub;
+        sel.qua = sel.qua || S.qua;
     }
     return sel;
 }
 
-// Resident CTAs (one replica each) or clusters that fit on the device at once.
-static int resident_slots(Ctx &C, int block, size_t *smem_out) {
+// Resident CTAs (one replica each) or clusters of a group that fit on the device at once.
+static int resident_slots(Ctx &C, const Group &G, int block, size_t *smem_out) {
     size_t smem = 0;
-    for (auto &S : C.sys) smem = std::max(smem, S->resident_smem);
-    const ResidentSel sel = resident_selection(C);
+    for (int k : G.sys) smem = std::max(smem, C.sys[k]->resident_smem);
+    const ResidentSel sel = resident_selection(C, G);
     const int cap = C.precision == CSMC_FP32 ? resident_capacity<float>(block, smem, sel, C.n_sms)
                                              : resident_capacity<double>(block, smem, sel, C.n_sms);
     require(cap >= 1, CSMC_ERR_UNSUPPORTED, "resident kernel does not fit on the device with this shared memory size");
@@ -923,41 +1026,68 @@ static int resident_slots(Ctx &C, int block, size_t *smem_out) {
     return cap;
 }
 
-// One resident launch.  rd.persistent: a cooperative launch with one CTA (or
-// cluster) per replica; returns false, with nothing launched, if the device
-// refuses it.
-static bool resident_launch(Ctx &C, RunDesc rd, int block, Launches &L) {
+// Is a persistent (cooperative, multi-window) launch possible: one group whose
+// replicas are all resident on the device at once.
+static bool persistent_fits(Ctx &C, int hint) {
+    if (C.groups.size() != 1) return false;
+    const Group &G = *C.groups[0];
+    return resident_slots(C, G, resident_block(C, G, hint), nullptr) >= G.n_items;
+}
+
+// One group's resident launch on stream `st`.
+static cudaError_t launch_group(Ctx &C, Group &G, RunDesc rd, int hint, cudaStream_t st) {
+    const int block = resident_block(C, G, hint);
     size_t smem = 0;
-    const int cap = resident_slots(C, block, &smem);
-    const ResidentSel sel = resident_selection(C);
+    const int cap = resident_slots(C, G, block, &smem);
+    const ResidentSel sel = resident_selection(C, G);
     // CTAs (one per replica) or clusters (sel.cl CTAs per replica)
-    const int grid = std::min(C.n_items, cap) * std::max(sel.cl, 1);
+    const int grid = std::min(G.n_items, cap) * std::max(sel.cl, 1);
     if (rd.persistent) {
-        require(cap >= C.n_items, CSMC_ERR_INVALID, "persistent launch needs every replica resident at once");
+        require(cap >= G.n_items, CSMC_ERR_INVALID, "persistent launch needs every replica resident at once");
         rd.grid_bar = C.grid_bar.p;
         rd.n_blocks = (uint32_t)grid;
         rd.lattices = C.lattices.p;
         rd.n_lattices = (int)C.sys.size();
         rd.k0 = C.k0;
         rd.k1 = C.k1;
-        CK(cudaMemsetAsync(C.grid_bar.p, 0, sizeof(unsigned int), C.st));
+        CK(cudaMemsetAsync(C.grid_bar.p, 0, sizeof(unsigned int), st));
     }
+    CK(cudaMemsetAsync(G.work_ctr.p, 0, sizeof(int), st));
+    return C.precision == CSMC_FP32
+               ? launch_resident<float>(C.fres.p, G.items.p, G.n_items, G.work_ctr.p, C.cs, rd, grid, block, smem,
+                                        sel, rd.persistent != 0, st)
+               : launch_resident<double>(C.dres.p, G.items.p, G.n_items, G.work_ctr.p, C.cs, rd, grid, block, smem,
+                                         sel, rd.persistent != 0, st);
+}
+
+// One resident launch of every replica (with size groups: one launch per
+// group, side by side on the groups' streams, joined back into the context's
+// stream).  rd.persistent: a cooperative launch with one CTA (or cluster) per
+// replica; returns false, with nothing launched, if the device refuses it.
+static bool resident_launch(Ctx &C, RunDesc rd, int hint, Launches &L) {
     auto ev = C.next_kernel_events();
-    CK(cudaMemsetAsync(C.work_ctr.p, 0, sizeof(int), C.st));
     CK(cudaEventRecord(ev.first, C.st));
-    cudaError_t e = C.precision == CSMC_FP32
-                        ? launch_resident<float>(C.fres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid, block,
-                                                 smem, sel, rd.persistent != 0, C.st)
-                        : launch_resident<double>(C.dres.p, C.items.p, C.n_items, C.work_ctr.p, C.cs, rd, grid,
-                                                  block, smem, sel, rd.persistent != 0, C.st);
-    if (e != cudaSuccess && rd.persistent) {
-        cudaGetLastError(); // a refused cooperative launch leaves no sticky error
-        C.kev_used--;
-        return false;
+    if (C.groups.size() == 1) {
+        const cudaError_t e = launch_group(C, *C.groups[0], rd, hint, C.st);
+        if (e != cudaSuccess && rd.persistent) {
+            cudaGetLastError(); // a refused cooperative launch leaves no sticky error
+            C.kev_used--;
+            return false;
+        }
+        CK(e);
+        L.n += 1;
+    } else {
+        require(!rd.persistent, CSMC_ERR_INVALID, "size groups run one launch per window");
+        CK(cudaEventRecord(C.fork, C.st));
+        for (auto &G : C.groups) {
+            CK(cudaStreamWaitEvent(G->st, C.fork, 0));
+            CK(launch_group(C, *G, rd, hint, G->st));
+            CK(cudaEventRecord(G->done, G->st));
+            L.n += 1;
+        }
+        for (auto &G : C.groups) CK(cudaStreamWaitEvent(C.st, G->done, 0));
     }
-    CK(e);
     CK(cudaEventRecord(ev.second, C.st));
-    L.n += 1;
     return true;
 }
 
@@ -1018,15 +1148,15 @@ static void run(Ctx &C, csmc_run_params *p) {
     };
 
     if (path == CSMC_PATH_RESIDENT) {
-        const int block = resident_block(C, p->resident_block);
+        const int hint = p->resident_block; // threads per CTA asked for (0: automatic)
+        require(hint >= 0 && hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
         // windows end at exchange iterations; without exchanges, at most
         // `chunk` iterations per launch.  With exchanges and every replica
         // resident at once, one persistent launch runs up to kWindows windows
         // and the exchanges between them.
         const int64_t chunk = 256, kWindows = 128;
         const int64_t period = s.swap_enabled ? std::lcm((int64_t)s.swap_rate, s.dosweep) : 0;
-        bool persistent = s.swap_enabled && C.persistent_on && C.persistent_ok &&
-                          resident_slots(C, block, nullptr) >= C.n_items;
+        bool persistent = s.swap_enabled && C.persistent_on && C.persistent_ok && persistent_fits(C, hint);
         int64_t it = s.start;
         while (it < s.end) {
             if (persistent) {
@@ -1051,7 +1181,7 @@ static void run(Ctx &C, csmc_run_params *p) {
                 rd.swap_enabled = 1;
                 rd.persistent = 1;
                 rd.swap_period = period;
-                if (!resident_launch(C, rd, block, L)) {
+                if (!resident_launch(C, rd, hint, L)) {
                     persistent = false; // the device refused the cooperative launch: one launch per window
                     C.persistent_ok = false;
                     continue;
@@ -1096,7 +1226,7 @@ static void run(Ctx &C, csmc_run_params *p) {
             rd.renorm_every = C.renorm_every;
             rd.sweeps0 = C.nsweeps;
             rd.swap_enabled = s.swap_enabled ? 1 : 0;
-            resident_launch(C, rd, block, L);
+            resident_launch(C, rd, hint, L);
             for (int64_t q = it; q <= to; q++) {
                 if (s.is_metro(q)) {
                     C.msweep++;
@@ -1194,7 +1324,7 @@ static void anneal(Ctx &C, const double *temps, int n_temps, int64_t t_therm, in
                 rd.n_slots = n_slots;
                 rd.renorm_every = C.renorm_every;
                 rd.sweeps0 = C.nsweeps;
-                resident_launch(C, rd, resident_block(C, 0), L);
+                resident_launch(C, rd, 0, L);
                 for (int64_t t = 1; t < t_therm; t++) {
                     if (t % dosweep == 0) {
                         C.msweep++;
@@ -1806,6 +1936,27 @@ int csmc_set_cluster_size(void *c, int32_t ranks) {
     API_END
 }
 
+int csmc_set_size_groups(void *c, int32_t on) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    CK(cudaStreamSynchronize(C.st));
+    if (on) make_size_groups(C);
+    else choose_cluster(C, 0);
+    bool ok = true;
+    for (auto &S : C.sys) ok = ok && S->resident_ok;
+    upload_resident(C);
+    require(ok || !on, CSMC_ERR_UNSUPPORTED, "a lattice of a size group does not fit the resident kernel");
+    API_END
+}
+
+int csmc_size_groups(void *c, int32_t *n_groups) {
+    API_BEGIN
+    Ctx &C = ctx_of(c);
+    require(n_groups != nullptr, CSMC_ERR_INVALID, "n_groups is NULL");
+    *n_groups = C.size_groups ? (int32_t)C.groups.size() : 0;
+    API_END
+}
+
 int csmc_cluster_size(void *c, int32_t *ranks) {
     API_BEGIN
     require(ranks != nullptr, CSMC_ERR_INVALID, "ranks is NULL");
@@ -1886,12 +2037,14 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
     const int span = q.swap_rate > 0 ? q.swap_rate : std::max(q.overrelaxation_rate, 1) * 10;
     q.n_sweeps = (int64_t)n_windows * span;
     const bool allow_persistent = C.persistent_on && C.persistent_ok; // csmc_set_persistent(0) is respected
+    const bool persistent0 = C.persistent_on;
     StateCopy saved(C);
     struct Cand {
         int cl, block;
         bool persistent;
         double ms;
         bool global = false;
+        bool groups = false; // size groups, each with its own launch shape
     };
     std::vector<Cand> cands;
     for (int cl : {1, 2, 4}) {
@@ -1905,8 +2058,9 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
         if (!ok) continue;
         upload_resident(C);
         C.block_pref = 0;
-        const ResidentSel sel = resident_selection(C);
-        const int balanced = resident_block(C, 0), largest = resident_max_threads(sel.fast, sel.bil, sel.ons);
+        const ResidentSel sel = resident_selection(C, *C.groups[0]);
+        const int balanced = resident_block(C, *C.groups[0], 0),
+                  largest = resident_max_threads(sel.fast, sel.bil, sel.ons);
         std::vector<int> blocks{balanced};
         if (largest != balanced) blocks.push_back(largest);
         for (int block : blocks) {
@@ -1920,6 +2074,27 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
                 cands.push_back({cl, block, pers && C.persistent_ok, C.last_ms / n_windows});
                 saved.restore(C);
             }
+        }
+    }
+    // lattices of very different sizes: size groups side by side, with the
+    // groups' CTAs uncapped or capped so that two or three share an SM
+    for (bool clusters : {true, false}) {
+        if (!make_size_groups(C, clusters)) break;
+        bool ok = true;
+        for (auto &S : C.sys) ok = ok && S->resident_ok;
+        if (!ok) continue;
+        upload_resident(C);
+        C.block_pref = 0;
+        C.persistent_on = persistent0;
+        for (int cap : {0, 448, 256}) {
+            C.group_block_cap = cap;
+            run(C, &q);
+            saved.restore(C);
+            run(C, &q);
+            Cand cg{clusters ? 0 : 1, cap, false, C.last_ms / n_windows};
+            cg.groups = true;
+            cands.push_back(cg);
+            saved.restore(C);
         }
     }
     require(!cands.empty(), CSMC_ERR_UNSUPPORTED, "no resident configuration fits these lattices");
@@ -1940,14 +2115,21 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
     size_t best_res = cands[best].global ? 0 : best; // resident configuration kept for explicit requests
     for (size_t k = 0; k < cands.size(); k++)
         if (!cands[k].global && cands[k].ms < cands[best_res].ms) best_res = k;
-    choose_cluster(C, cands[best_res].cl);
+    if (cands[best_res].groups) {
+        make_size_groups(C, cands[best_res].cl == 0);
+        C.persistent_on = persistent0;
+        C.group_block_cap = cands[best_res].block;
+        C.block_pref = 0;
+    } else {
+        choose_cluster(C, cands[best_res].cl);
+        C.persistent_on = cands[best_res].persistent;
+        C.block_pref = cands[best_res].block;
+    }
     upload_resident(C);
-    C.block_pref = cands[best_res].block;
-    C.persistent_on = cands[best_res].persistent;
     C.global_pref = cands[best].global;
     for (size_t k = 0; k < cands.size() && (int)k < capacity; k++) {
         out[k].path = cands[k].global ? CSMC_PATH_GLOBAL : CSMC_PATH_RESIDENT;
-        out[k].cluster = cands[k].cl;
+        out[k].cluster = cands[k].groups ? -cands[k].cl : cands[k].cl; // size groups: 0 or -1
         out[k].block = cands[k].block;
         out[k].persistent = cands[k].persistent ? 1 : 0;
         out[k].ms_per_window = cands[k].ms;

@@ -845,6 +845,11 @@ __global__ void __launch_bounds__(NT, 1)
             const double T = s_T;
             const R invT = s_invT;
             double acc_total = 0.0;
+            // accepted proposals of this thread's sites: summed over the block
+            // (and cluster) after every Metropolis sweep when the adaptive
+            // kind needs the rate, else once at the end of the window
+            const bool adaptive = rd.kind == CSMC_METROPOLIS_ADAPTIVE;
+            unsigned acc_thread = 0;
 
             for (int64_t it = w0; it < w1; it++) {
                 if (rd.or_rate != 0) {
@@ -868,17 +873,19 @@ __global__ void __launch_bounds__(NT, 1)
                                                : k.template metro_sweep<false>(rd.kind, (R)s_sigma, invT, T, msweep);
                     msweep++;
                     sweeps++;
-                    const double at = sync.sum(a); // exact: an integer sum per warp
-                    if (threadIdx.x == 0) {
-                        acc_total += at;
-                        if (rd.kind == CSMC_METROPOLIS_ADAPTIVE) { // metropolis.jl:124-126
+                    if (adaptive) {
+                        const double at = sync.sum(a); // exact: an integer sum per warp
+                        if (threadIdx.x == 0) { // metropolis.jl:124-126
+                            acc_total += at;
                             const double om = 1 - at / (double)S.n_real;
                             const double f = 0.5 / (om > 0.05 ? om : 0.05);
                             double sg = s_sigma * f;
                             s_sigma = sg < 0.0 ? 0.0 : (sg > 100 ? 100 : sg);
                         }
+                        __syncthreads();
+                    } else {
+                        acc_thread += a;
                     }
-                    __syncthreads();
                     if (measure) {
                         double o[4];
                         sync.sum4(meas[0], meas[1], meas[2], meas[3], o);
@@ -910,6 +917,10 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
 
+            if (!adaptive) {
+                const double at = sync.sum(acc_thread);
+                if (threadIdx.x == 0) acc_total = at;
+            }
             if (writer) {
                 cs.E_chain[c] = E;
                 cs.acc_slot[slot] = __ldcg(cs.acc_slot + slot) + acc_total;

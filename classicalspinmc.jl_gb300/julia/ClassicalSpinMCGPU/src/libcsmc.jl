@@ -233,6 +233,12 @@ function c_cluster_size(ctx)
     check(ccall((:csmc_cluster_size, libcsmc), Cint, (Ptr{Cvoid}, Ref{Int32}), ctx, r))
     Int(r[])
 end
+c_set_size_groups(ctx, on::Bool) = check(ccall((:csmc_set_size_groups, libcsmc), Cint, (Ptr{Cvoid}, Int32), ctx, on))
+function c_size_groups(ctx)
+    r = Ref{Int32}(0)
+    check(ccall((:csmc_size_groups, libcsmc), Cint, (Ptr{Cvoid}, Ref{Int32}), ctx, r))
+    Int(r[])
+end
 c_structure_factor(ctx, lattice::Integer, dim::Integer, positions::Matrix{Float64}, ks::Matrix{Float64},
                    Suv::Array{Float64,3}) =
     check(ccall((:csmc_structure_factor, libcsmc), Cint,

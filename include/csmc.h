@@ -318,7 +318,24 @@ int csmc_anneal(void *ctx, const double *temps, int32_t n_temps, int64_t t_therm
  * basis per colour class (CSMC_ERR_UNSUPPORTED otherwise).  A tuning knob of
  * this library; no counterpart in the reference. */
 int csmc_set_cluster_size(void *ctx, int32_t ranks);
+/* The cluster size in use; 0 while size groups are in use (each group has its own). */
 int csmc_cluster_size(void *ctx, int32_t *ranks);
+
+/* Size groups for batches of lattices of very different sizes (a scheduling
+ * knob of this library; no counterpart in the reference, which runs one
+ * lattice per MPI rank).  On: the lattices are sorted by size and split
+ * wherever the size drops below half of the group's largest; each group gets
+ * its own resident launch shape -- cluster size as csmc_set_cluster_size(0)
+ * picks it for that group alone, and threads per CTA balanced for its largest
+ * colour class -- and the groups' launches run side by side on streams of
+ * their own, so small replicas run as small CTAs several to an SM while the
+ * largest are split over clusters.  Every window is then one launch per group
+ * (no persistent multi-window launches).  Off: one launch shape for the whole
+ * context (the default; csmc_set_cluster_size also turns size groups off).
+ * Chains are the same either way.  csmc_size_groups reports the number of
+ * groups in use (0: off). */
+int csmc_set_size_groups(void *ctx, int32_t on);
+int csmc_size_groups(void *ctx, int32_t *n_groups);
 
 /* compute_equal_time_correlations (spin_correlations.jl:6-43) for every slot
  * of lattice `lattice`: S_a(k) = sum_i exp(-i k.r_i) s_i,a and
@@ -357,7 +374,8 @@ int csmc_persistent(void *ctx, int32_t *on);
  * tuning knobs are this library's).  For every cluster size that fits (1, 2
  * or 4 CTAs per replica), two block sizes (the balanced one and the resident
  * kernel's largest), persistent windows on and off (see csmc_set_persistent)
- * and, when params->path is CSMC_PATH_AUTO, the global colour-sweep path, it
+ * size groups when the lattices' sizes differ by more than a factor two, and,
+ * when params->path is CSMC_PATH_AUTO, the global colour-sweep path, it
  * times n_windows exchange windows of the
  * schedule in *params on the context's own replicas, restores the replicas and
  * every counter exactly (the chain continues as if no tuning had happened),
@@ -367,8 +385,9 @@ int csmc_persistent(void *ctx, int32_t *on);
  * number of candidates (0 when the lattices run on the global path). */
 typedef struct {
     int32_t path;          /* CSMC_PATH_RESIDENT or CSMC_PATH_GLOBAL */
-    int32_t cluster;       /* CTAs per replica (resident) */
-    int32_t block;         /* threads per CTA */
+    int32_t cluster;       /* CTAs per replica (resident); size groups (csmc_set_size_groups): 0 with
+                              each group's own cluster size, -1 with one CTA per replica throughout */
+    int32_t block;         /* threads per CTA; size groups: the cap on every group's CTAs (0: none) */
     int32_t persistent;    /* 1: windows and exchanges in one cooperative launch */
     double ms_per_window;  /* device time of one exchange window */
     int32_t chosen;        /* 1 for the configuration kept */

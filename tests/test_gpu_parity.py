@@ -341,13 +341,14 @@ def test_honeycomb_anneal_kat(m, orc, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("path", ["resident", "global"])
+@pytest.mark.parametrize("path", ["resident", "size_groups", "global"])
 def test_batch_of_lattices_matches_single(m, orc, precision, path):
     """Independent chains of different sizes in one context (the uneven batch
     of independent chains) == each chain run alone: with the same chain id
     (csmc_set_chain_ids), seed and initial spins, a chain draws the same
     numbers wherever it runs, so its spins and accepted counts agree bit for
-    bit.  The batch runs every lattice in one launch (one work list); alone,
+    bit.  The batch runs every lattice in one launch (one work list), or as
+    size groups (one launch shape per band of sizes, side by side); alone,
     each context picks its own launch shape."""
     import ctypes as C
     from importlib import import_module
@@ -363,13 +364,18 @@ def test_batch_of_lattices_matches_single(m, orc, precision, path):
         ctx.call("csmc_set_chain_ids", ids_.ctypes.data_as(C.POINTER(C.c_uint32)))
         rp = L.RunParams()
         rp.sweep_start, rp.n_sweeps, rp.overrelaxation_rate = 1, 30, 3
-        rp.path = {"resident": L.PATH_RESIDENT, "global": L.PATH_GLOBAL}[path]
+        rp.path = L.PATH_GLOBAL if path == "global" else L.PATH_RESIDENT
         acc = np.zeros(ctx.n_slots)
         rp.accepted = acc.ctypes.data_as(C.POINTER(C.c_double))
         ctx.call("csmc_run", C.byref(rp))
         return acc
 
     batch = m.monte_carlo.Context(lats, [1] * len(lats), precision=precision, seed=4)
+    if path == "size_groups":
+        batch.call("csmc_set_size_groups", 1)
+        n = C.c_int32()
+        batch.call("csmc_size_groups", C.byref(n))
+        assert n.value >= 2  # padded sizes of about 600 and 400 | 220 and 130
     for k, lat in enumerate(lats):
         batch.set_spins(k, lat.spins)
     acc_b = run(batch, Ts, ids)
