@@ -125,6 +125,7 @@ SIGNATURES = {
     "csmc_size_groups": (C.c_int, [_vp, i32p]),
     "csmc_autotune": (C.c_int, [_vp, C.POINTER(RunParams), C.c_int32, C.POINTER(TuneEntry), C.c_int32, i32p]),
     "csmc_structure_factor": (C.c_int, [_vp, C.c_int32, C.c_int32, f64p, C.c_int64, f64p, f64p]),
+    "csmc_set_tensor_cores": (C.c_int, [_vp, C.c_int32]),
     "csmc_selftest_timeout": (C.c_int, [_vp, C.c_int32]),
     "csmc_set_persistent": (C.c_int, [_vp, C.c_int32]),
     "csmc_persistent": (C.c_int, [_vp, i32p]),

@@ -156,6 +156,7 @@ struct Ctx {
     int n_items = 0;       // replicas of every lattice
     std::vector<std::unique_ptr<Group>> groups; // one, or the size groups
     bool size_groups = false;                   // csmc_set_size_groups / the autotuner's choice
+    bool sf_tensor = true; // single-precision structure factors on the tensor cores (csmc_set_tensor_cores)
     int group_block_cap = 0; // size groups: at most this many threads per CTA (0: none), so CTAs of
                              // several groups share an SM (the autotuner's choice)
     cudaEvent_t fork = nullptr;                 // size groups start after the work queued before them
@@ -1367,7 +1368,10 @@ template <typename R>
 static void structure_factor(Ctx &C, System &S, const SysArgs<R> &a, int dim, const double *positions, int64_t n_k,
                              const double *ks, double *Suv) {
     const Plan &P = S.plan;
-    std::vector<R> pd((size_t)P.Np * 3, R(0)), kd((size_t)std::max<int64_t>(n_k, 1) * 3, R(0));
+    // single precision on the tensor cores (positions padded to whole chunks of sites)
+    const bool tensor = sizeof(R) == 4 && C.sf_tensor;
+    const int64_t n_pos = tensor ? sf_tc_sites(P.Np) : P.Np;
+    std::vector<R> pd((size_t)n_pos * 3, R(0)), kd((size_t)std::max<int64_t>(n_k, 1) * 3, R(0));
     for (int64_t d = 0; d < P.Np; d++) {
         const int64_t i = P.dev2ref[d];
         if (i < 0) continue;
@@ -1383,7 +1387,15 @@ static void structure_factor(Ctx &C, System &S, const SysArgs<R> &a, int dim, co
     C.reset_kernel_time();
     auto ev = C.next_kernel_events();
     CK(cudaEventRecord(ev.first, C.st));
-    launch_structure_factor<R>(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, C.st);
+    DevBuf<float> packed;
+    if constexpr (sizeof(R) == 4) {
+        if (tensor) {
+            packed.alloc((size_t)sf_tc_packed_floats(P.Np, S.R));
+            CK(launch_structure_factor_tc(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, packed.p,
+                                          C.error_flag.p, C.st));
+        }
+    }
+    if (!tensor) launch_structure_factor<R>(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, C.st);
     CK(cudaEventRecord(ev.second, C.st));
     sync_check(C);
     C.collect_kernel_time();
@@ -2164,6 +2176,12 @@ int csmc_structure_factor(void *c, int32_t lattice, int32_t dim, const double *p
     CK(cudaStreamSynchronize(C.st));
     if (C.precision == CSMC_FP32) structure_factor<float>(C, S, S.fa, dim, positions, n_k, ks, Suv);
     else structure_factor<double>(C, S, S.da, dim, positions, n_k, ks, Suv);
+    API_END
+}
+
+int csmc_set_tensor_cores(void *c, int32_t on) {
+    API_BEGIN
+    ctx_of(c).sf_tensor = on != 0;
     API_END
 }
 

@@ -280,6 +280,49 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     }
 }
 
+// The bilinear fields hb of two sites d0, d1 of a lattice without cubic and
+// quartic terms, spins in global memory: per group of three slots, both
+// sites' partner indices, then both sites' partner spins are loaded before
+// any is used, so twice as many gathers are in flight per dependent step.
+// Each site's sum is formed in partner_fields' order (bit for bit the same).
+template <typename R, class SV>
+__device__ __forceinline__ void bilinear_fields2(const Tab<uint32_t> &tb, const Coef<R> &cf, const SV &sv, int d0,
+                                                 int d1, int b0, int b1, V3<R> &hb0, V3<R> &hb1) {
+    hb0 = {R(0), R(0), R(0)};
+    hb1 = {R(0), R(0), R(0)};
+    const int Np = (int)tb.Np;
+    auto bil = [&](int b, int t, V3<R> sj, V3<R> &hb) {
+        const int id = cf.c2[b * tb.W2 + t];
+        if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sj); // J I
+        else hb = add_matvec(hb, cf.mats + 9 * id, sj);
+    };
+    constexpr int G = 3;
+    int t = 0;
+    for (; t + G <= tb.W2; t += G) {
+        int j0[G], j1[G];
+        V3<R> s0[G], s1[G];
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            j0[u] = (int)tb.p2[(t + u) * Np + d0];
+            j1[u] = (int)tb.p2[(t + u) * Np + d1];
+        }
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            s0[u] = sv.get(j0[u]);
+            s1[u] = sv.get(j1[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < G; u++) bil(b0, t + u, s0[u], hb0);
+#pragma unroll
+        for (int u = 0; u < G; u++) bil(b1, t + u, s1[u], hb1);
+    }
+    for (; t < tb.W2; t++) {
+        const V3<R> s0r = sv.get(tb.p2[t * Np + d0]), s1r = sv.get(tb.p2[t * Np + d1]);
+        bil(b0, t, s0r, hb0);
+        bil(b1, t, s1r, hb1);
+    }
+}
+
 template <typename R> __device__ __forceinline__ V3<R> matvec(const R *M, V3<R> s) {
     using F = Fp<R>;
     return {F::fma(M[2], s.z, F::fma(M[1], s.y, F::mul(M[0], s.x))),
@@ -291,16 +334,22 @@ template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) {
     return F::fma(a.z, b.z, F::fma(a.y, b.y, F::mul(a.x, b.x)));
 }
 
-// get_local_field (hamiltonian.jl:3-67): 2 O s + (self loops) + partners - h.
-template <typename R, typename Idx, bool CUB, bool QUA, class SV>
-__device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b) {
-    V3<R> hb, hc, hq;
-    partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
-    const V3<R> s = sv.get(d);
+// get_local_field (hamiltonian.jl:3-67) of site spin s of pattern b from its
+// partners' fields: 2 O s + (self loops) + hb + hc + hq - h.
+template <typename R>
+__device__ __forceinline__ V3<R> field_of(const Coef<R> &cf, int b, V3<R> s, V3<R> hb, V3<R> hc, V3<R> hq) {
     const V3<R> os = matvec(cf.O + 9 * b, s), ps = matvec(cf.P + 9 * b, s);
     const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
     const V3<R> two_os = {Fp<R>::mul(R(2), os.x), Fp<R>::mul(R(2), os.y), Fp<R>::mul(R(2), os.z)};
     return vsub(vadd(vadd(vadd(vadd(two_os, ps), hb), hc), hq), h);
+}
+
+// get_local_field (hamiltonian.jl:3-67) at device site d.
+template <typename R, typename Idx, bool CUB, bool QUA, class SV>
+__device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b) {
+    V3<R> hb, hc, hq;
+    partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
+    return field_of(cf, b, sv.get(d), hb, hc, hq);
 }
 
 // Energy of moving site d from s to sn with all other spins fixed:

@@ -66,6 +66,14 @@ void launch_structure_factor(const SysArgs<R> &a, const R *pos, const R *ks, int
                              int slot_base, double *out, cudaStream_t st);
 // Philox4x32-10 of n counters (4 words each) under n keys (2 words each)
 void launch_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t *out, cudaStream_t st);
+// the same on the tensor cores for a single-precision lattice (correlations_tc.cu):
+// pos 3 per device site for sf_tc_sites(Np) sites (zero-padded), packed
+// sf_tc_packed_floats(Np, n_rep) floats of scratch for the split spins
+int64_t sf_tc_sites(int64_t Np);
+int64_t sf_tc_packed_floats(int64_t Np, int n_rep);
+cudaError_t launch_structure_factor_tc(const SysArgs<float> &a, const float *pos, const float *ks, int64_t n_k,
+                                       const int32_t *slot_of, int slot_base, double *out, float *packed,
+                                       int *error_flag, cudaStream_t st);
 // a kernel whose bounded wait cannot complete (see csmc_selftest_timeout)
 cudaError_t launch_wait_selftest(int which, unsigned int *ctr, int *error_flag, cudaStream_t st);
 // static shared memory of the selected resident kernel in bytes (-1: query failed)

@@ -244,6 +244,7 @@ c_structure_factor(ctx, lattice::Integer, dim::Integer, positions::Matrix{Float6
     check(ccall((:csmc_structure_factor, libcsmc), Cint,
                 (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}),
                 ctx, lattice, dim, positions, size(ks, 2), ks, Suv))
+c_set_tensor_cores(ctx, on::Bool) = check(ccall((:csmc_set_tensor_cores, libcsmc), Cint, (Ptr{Cvoid}, Int32), ctx, on))
 c_selftest_timeout(ctx, which::Integer) =
     ccall((:csmc_selftest_timeout, libcsmc), Cint, (Ptr{Cvoid}, Int32), ctx, which)
 c_set_persistent(ctx, on::Bool) = check(ccall((:csmc_set_persistent, libcsmc), Cint, (Ptr{Cvoid}, Int32), ctx, on))

@@ -349,6 +349,14 @@ int csmc_size_groups(void *ctx, int32_t *n_groups);
 int csmc_structure_factor(void *ctx, int32_t lattice, int32_t dim, const double *positions, int64_t n_k,
                           const double *ks, double *Suv);
 
+/* Single-precision structure factors (csmc_structure_factor of a CSMC_FP32
+ * context) on the tensor cores (on, the default: tcgen05 TF32 matrix
+ * multiplies with each operand split into two TF32 halves, FP32 accumulation)
+ * or on the CUDA cores (off: FP32 fused multiply-adds).  A choice of this
+ * library; no counterpart in the reference.  Double-precision contexts always
+ * use the CUDA cores. */
+int csmc_set_tensor_cores(void *ctx, int32_t on);
+
 /* Self-test of the bounded device waits (no counterpart in the reference).
  * Runs a kernel whose wait can never complete -- which = 0: an mbarrier phase
  * waiting for 16 bytes no copy delivers; which = 1: a grid barrier expecting

@@ -107,3 +107,35 @@ def test_parallel_tempering_saves_initial_configurations(m, orc):
             s = ics[r][ts]
             assert ol.total_energy(s) == pytest.approx(out["energy"][k, r], rel=1e-12, abs=1e-12)
             assert ol.magnetization(s) == pytest.approx(out["magnetization"][k, r], rel=1e-12, abs=1e-12)
+
+
+@pytest.mark.parametrize("name,shape,R,n_k,aligned", [("sc", (4, 4, 4), 17, 77, False), ("sc", (6, 6, 6), 70, 130, False),
+                                                       ("square", (8, 8), 3, 200, False), ("sc", (6, 6, 6), 5, 40, True),
+                                                       ("pyrochlore", (2, 2, 3), 1, 129, False)])
+def test_tensor_core_structure_factor(m, orc, name, shape, R, n_k, aligned):
+    """Single precision on the tensor cores (tcgen05, each operand split into
+    two TF32 halves) against the oracle and against the CUDA-core kernel, with
+    the FP32 tolerance 2e-5 x N: wavevector counts that are not multiples of
+    the 128-wavevector tile, more than 64 replicas (two replica tiles), and all
+    spins aligned (|S(0)|^2 / N = N, the largest sums)."""
+    E = m.examples
+    uc = {"square": E.square_heisenberg, "sc": E.sc_heisenberg, "pyrochlore": E.pyrochlore_ckq}[name]()
+    lat = m.Lattice(shape, uc, 1.0)
+    mc = m.MonteCarlo([0.5 + 0.01 * r for r in range(R)] if R > 1 else 0.5, lat, {}, precision="fp32", seed=5)
+    for r in range(R):
+        s = rand_spins(lat.size, 300 + r)
+        if aligned:
+            s = np.asfortranarray(np.tile(s[:, :1], (1, lat.size)))
+        mc.set_spins(s, r)
+    ks = _wavevectors(lat, n_k, 8)
+    tc = m.structure_factors(mc, ks)
+    mc.ctx.call("csmc_set_tensor_cores", 0)
+    cc = m.structure_factors(mc, ks)
+    mc.ctx.call("csmc_set_tensor_cores", 1)
+    tol = TOL["fp32"] * lat.size
+    assert np.abs(tc - cc).max() <= tol, np.abs(tc - cc).max()
+    for r in range(R):
+        ref = orc.structure_factor(mc.spins(r), lat.site_positions, ks)
+        assert np.abs(tc[r] - ref).max() <= tol, (r, np.abs(tc[r] - ref).max())
+    if aligned:
+        assert tc[0][0, 0] + tc[0][4, 0] + tc[0][8, 0] == pytest.approx(lat.size, rel=1e-5)
