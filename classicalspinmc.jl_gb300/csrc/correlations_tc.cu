@@ -12,19 +12,21 @@
 //
 // One CTA: 128 wavevectors (the MMA's M) x 64 replicas (N = 192 columns:
 // replica-major, x y z), the sites in chunks of 16 (two MMA K-steps of 8).
-// Per chunk, all threads evaluate the 128 x 16 phases (range-reduced
-// hardware sincos) and store their TF32 halves in shared memory in the
-// no-swizzle K-major core-matrix layout; the spins, split and laid out the
-// same way beforehand by k_sf_pack (one layout for every wavevector tile),
-// arrive by bulk copies issued two chunks ahead (four spin buffers).  One
-// thread issues the chunk's 12 MMAs (cos and sin, three products, two
-// K-steps) and commits them to the phase stage's mbarrier; the threads
-// meanwhile fill the other phase stage.  The accumulators
-// (cos sums in TMEM columns 0..191, sin sums in 256..447) are read back with
-// tcgen05.ld and turned into the nine products in FP64.
+// Warp-specialised pipeline, synchronised by mbarriers only:
+//  * 16 producer warps evaluate each chunk's 128 x 16 phases (range-reduced
+//    hardware sincos) and store their TF32 halves in shared memory in the
+//    no-swizzle K-major core-matrix layout (three phase stages; a quarter-warp
+//    writes one 128-byte core-matrix column, so the stores are conflict-free);
+//  * one issuer warp brings each chunk's spins -- split and laid out the same
+//    way beforehand by k_sf_pack, one layout for every wavevector tile -- and
+//    the chunk's site positions by one bulk copy two chunks ahead (four
+//    buffers), and, once the chunk's phases are written, issues its 12 MMAs
+//    (cos and sin, three products, two K-steps) and commits them.
+// The accumulators (cos sums in TMEM columns 0..191, sin sums in 256..447)
+// are read back with tcgen05.ld and turned into the nine products in FP64.
 //
 // Every wait is bounded (one second of %globaltimer): on a timeout the CTA
-// sets the error flag, waits (bounded) for the copy and the MMAs it issued,
+// sets the error flag, waits (bounded) for the copies and the MMAs it issued,
 // frees its tensor memory and returns.
 #include "launch.hpp"
 
@@ -32,25 +34,27 @@ namespace csmc {
 
 namespace {
 
-constexpr int TC_THREADS = 256;
-constexpr int TC_M = 128;            // wavevectors per CTA (MMA M)
-constexpr int TC_R = 64;             // replicas per CTA
-constexpr int TC_N = 3 * TC_R;       // MMA N: 192 spin columns
-constexpr int TC_K = 16;             // sites per chunk
-constexpr int TC_CORES_K = TC_K / 4; // 16-byte core-matrix columns per chunk (4 TF32 each)
-constexpr uint32_t A_BYTES = TC_M * TC_K * 4; // one A operand (cos or sin, hi or lo): 8 KB
-constexpr uint32_t B_BYTES = TC_N * TC_K * 4; // one B operand (hi or lo): 12 KB
-constexpr uint32_t A_STAGE = 4 * A_BYTES; // cos hi|lo, sin hi|lo of one chunk: 32 KB
-constexpr uint32_t B_STAGE = 2 * B_BYTES; // spins hi|lo of one chunk: 24 KB
-constexpr int A_STAGES = 2;               // phases: written while the other stage's MMAs run
-constexpr int B_STAGES = 4;               // spins: each copied two chunks ahead of its MMAs
-constexpr int B_AHEAD = 2;
-constexpr uint32_t TC_SMEM = A_STAGES * A_STAGE + B_STAGES * B_STAGE; // 160 KB: one CTA per SM, which
+constexpr int TC_PRODUCERS = 512;                 // 16 warps evaluating phases
+constexpr int TC_THREADS = TC_PRODUCERS + 32;      // and one warp issuing copies and MMAs
+constexpr int TC_M = 128;                          // wavevectors per CTA (MMA M)
+constexpr int TC_R = 64;                           // replicas per CTA
+constexpr int TC_N = 3 * TC_R;                     // MMA N: 192 spin columns
+constexpr int TC_K = 16;                           // sites per chunk
+constexpr int TC_CORES_K = TC_K / 4;               // 16-byte core-matrix columns per chunk (4 TF32 each)
+constexpr uint32_t A_BYTES = TC_M * TC_K * 4;      // one A operand (cos or sin, hi or lo): 8 KB
+constexpr uint32_t B_BYTES = TC_N * TC_K * 4;      // one B operand (hi or lo): 12 KB
+constexpr uint32_t POS_BYTES = TC_K * 16;          // the chunk's site positions, x y z 0 per site
+constexpr uint32_t A_STAGE = 4 * A_BYTES;          // cos hi|lo, sin hi|lo of one chunk: 32 KB
+constexpr uint32_t B_STAGE = 2 * B_BYTES + POS_BYTES; // spins hi|lo and positions of one chunk
+constexpr int TILE_FLOATS = (int)(B_STAGE / 4);    // one chunk of k_sf_pack's output
+constexpr int A_STAGES = 3;
+constexpr int B_STAGES = 4;
+constexpr int B_AHEAD = 2; // a chunk's copy is issued while the MMAs of the chunk two before it run
+constexpr uint32_t TC_SMEM = A_STAGES * A_STAGE + B_STAGES * B_STAGE; // 193 KB: one CTA per SM, which
                                                                       // takes all 512 TMEM columns
-// the copy of chunk c + B_AHEAD, issued after the MMAs of chunk c - A_STAGES
-// are complete, reuses the buffer of chunk c + B_AHEAD - B_STAGES, which must
-// be at most chunk c - A_STAGES
-static_assert(B_STAGES >= A_STAGES + B_AHEAD, "a spin buffer is refilled only after the MMAs that read it");
+// the copy of chunk c + B_AHEAD reuses the buffer of chunk c + B_AHEAD - B_STAGES,
+// whose MMAs the issuer waits for; that chunk must precede c
+static_assert(B_STAGES > B_AHEAD, "a spin buffer is refilled only after the MMAs that read it");
 constexpr uint32_t TMEM_COLS = 512; // cos 0..191, sin 256..447
 constexpr uint32_t SIN_COL = 256;
 constexpr uint64_t TC_BUDGET_NS = 1000000000ull;
@@ -134,10 +138,12 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[24], int 
 // The spins of every replica of a lattice as the MMA's B operand: for replica
 // tile rt (64 replicas) and chunk c (16 device sites), the TF32 halves hi |
 // lo of the [192 x 16] K-major tile (column 3 r + a = component a of replica
-// r), each in the core-matrix layout; zero beyond the lattice's sites and
-// replicas.  packed holds n_rt x n_chunks x 2 x 3072 floats.
-__global__ void k_sf_pack(const float *__restrict__ spins, int64_t Np, int n_rep, int n_chunks,
-                          float *__restrict__ packed) {
+// r), each in the core-matrix layout, zero beyond the lattice's sites and
+// replicas; then the chunk's 16 site positions (x y z 0).  packed holds
+// n_rt x n_chunks x TILE_FLOATS floats; pos has 3 floats per device site for
+// n_chunks x TC_K sites.
+__global__ void k_sf_pack(const float *__restrict__ spins, const float *__restrict__ pos, int64_t Np, int n_rep,
+                          int n_chunks, float *__restrict__ packed) {
     // one (chunk, column, site) of replica tile blockIdx.y per thread
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (int64_t)n_chunks * TC_N * TC_K) return;
@@ -150,33 +156,39 @@ __global__ void k_sf_pack(const float *__restrict__ spins, int64_t Np, int n_rep
     float v = 0.f;
     if (r < n_rep && i < Np) v = spins[((int64_t)r * Np + i) * 4 + a];
     const float hi = to_tf32(v), lo = to_tf32(v - hi);
-    float *tile = packed + ((int64_t)rt * n_chunks + c) * (2 * TC_N * TC_K);
+    float *tile = packed + ((int64_t)rt * n_chunks + c) * TILE_FLOATS;
     const uint32_t off = core_offset(n, kel) / 4;
     tile[off] = hi;
     tile[TC_N * TC_K + off] = lo;
+    if (n == 0)
+        reinterpret_cast<float4 *>(tile + 2 * TC_N * TC_K)[kel] =
+            make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
 }
 
-// pos: 3 per device site for n_chunks x TC_K sites (zero beyond the lattice's
-// Np); ks: 3 per wavevector; packed: k_sf_pack's tiles; out[slot][k][9].
+// ks: 3 per wavevector; packed: k_sf_pack's tiles; out[slot][k][9].
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_structure_factor_tc(const float *__restrict__ packed, int n_chunks, int n_rep, const float *__restrict__ pos,
-                          const float *__restrict__ ks, int64_t n_k, int64_t n_real,
-                          const int32_t *__restrict__ slot_of, int chain_base, int slot_base, double *__restrict__ out,
-                          int *error_flag) {
+    k_structure_factor_tc(const float *__restrict__ packed, int n_chunks, int n_rep, const float *__restrict__ ks,
+                          int64_t n_k, int64_t n_real, const int32_t *__restrict__ slot_of, int chain_base,
+                          int slot_base, double *__restrict__ out, int *error_flag) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t bar_b[B_STAGES], bar_mma[A_STAGES];
+    __shared__ uint64_t bar_b[B_STAGES], bar_full[A_STAGES], bar_mma[A_STAGES];
     __shared__ uint32_t s_tmem;
     __shared__ int s_fail, s_issued;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool producer = tid < TC_PRODUCERS;
     const int64_t k0 = (int64_t)blockIdx.x * TC_M;
     const int rt = blockIdx.y;
     unsigned char *const a_st = smem;                       // A_STAGES x (cos hi, cos lo, sin hi, sin lo)
-    unsigned char *const b_st = smem + A_STAGES * A_STAGE; // B_STAGES x (spins hi, spins lo)
+    unsigned char *const b_st = smem + A_STAGES * A_STAGE; // B_STAGES x (spins hi, spins lo, positions)
 
     if (tid == 0) {
         for (int q = 0; q < B_STAGES; q++) mbar_init_(&bar_b[q], 1);
-        for (int q = 0; q < A_STAGES; q++) mbar_init_(&bar_mma[q], 1);
+        for (int q = 0; q < A_STAGES; q++) {
+            mbar_init_(&bar_full[q], TC_PRODUCERS);
+            mbar_init_(&bar_mma[q], 1);
+        }
         s_fail = 0;
+        s_issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) { // the accumulators: 512 columns of tensor memory
@@ -189,121 +201,116 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
+    const float *tiles = packed + (int64_t)rt * n_chunks * TILE_FLOATS;
 
-    // this thread's wavevector and half of each chunk's sites
-    const int kk = tid >> 1, half = tid & 1;
-    const int64_t k = k0 + kk;
-    float kx = 0.f, ky = 0.f, kz = 0.f;
-    if (k < n_k) {
-        kx = ks[3 * k];
-        ky = ks[3 * k + 1];
-        kz = ks[3 * k + 2];
-    }
-    const float *tiles = packed + (int64_t)rt * n_chunks * (2 * TC_N * TC_K);
-    int issued = 0;  // chunks whose MMAs thread 0 has issued
-    int copied = -1; // the last chunk whose spins thread 0 has requested by bulk copy
-    int landed = -1; // the last chunk whose copy thread 0 has seen complete
-    // the spins of chunk cc into its buffer by one bulk copy (thread 0)
-    auto copy_spins = [&](int cc) {
-        const int q = cc % B_STAGES;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b[q])),
-                     "r"(B_STAGE)
-                     : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         smem_addr(b_st + q * B_STAGE)),
-                     "l"(tiles + (int64_t)cc * (2 * TC_N * TC_K)), "r"(B_STAGE), "r"(smem_addr(&bar_b[q]))
-                     : "memory");
-        copied = cc;
-    };
-    if (tid == 0)
-        for (int cc = 0; cc < B_AHEAD && cc < n_chunks; cc++) copy_spins(cc);
-
-    for (int c = 0; c < n_chunks; c++) {
-        const int s = c % A_STAGES;
-        unsigned char *st = a_st + s * A_STAGE;
-        // the MMAs of chunk c - 2 have finished reading phase stage s and the
-        // spin buffer that chunk c + 2 is copied into
-        if (c >= A_STAGES) {
-            const bool ok = mbar_wait(&bar_mma[s], (uint32_t)(((c - A_STAGES) / A_STAGES) & 1));
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) s_fail = 1;
+    if (producer) {
+        // row (wavevector) and core-matrix column (4 sites) of this thread: a
+        // quarter-warp covers 8 consecutive rows of one column, 128 contiguous bytes
+        const int row = 8 * warp + (lane & 7), q4 = lane >> 3;
+        const int64_t k = k0 + row;
+        float kx = 0.f, ky = 0.f, kz = 0.f;
+        if (k < n_k) {
+            kx = ks[3 * k];
+            ky = ks[3 * k + 1];
+            kz = ks[3 * k + 2];
+        }
+        const uint32_t off = core_offset(row, 4 * q4);
+        for (int c = 0; c < n_chunks; c++) {
+            const int s = c % A_STAGES, q = c % B_STAGES;
+            bool ok = mbar_wait(&bar_b[q], (uint32_t)((c / B_STAGES) & 1)); // the chunk's positions
+            if (ok && c >= A_STAGES) // the MMAs of chunk c - A_STAGES have read this phase stage
+                ok = mbar_wait(&bar_mma[s], (uint32_t)(((c - A_STAGES) / A_STAGES) & 1));
+            if (!ok || *(volatile int *)&s_fail) {
+                s_fail = 1;
                 break;
             }
-        }
-        if (tid == 0 && c + B_AHEAD < n_chunks) copy_spins(c + B_AHEAD);
-        // the phases of this thread's wavevector at sites 8 half .. 8 half + 7 of the chunk
-        float cs[8], sn[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int64_t i = (int64_t)c * TC_K + 8 * half + q;
-            const float t = __fmaf_rn(kz, pos[3 * i + 2], __fmaf_rn(ky, pos[3 * i + 1], __fmul_rn(kx, pos[3 * i])));
-            sincos_tc(t, &sn[q], &cs[q]);
-        }
-#pragma unroll
-        for (int g = 0; g < 2; g++) { // two core-matrix columns of 4 sites
+            const float4 *p4 = reinterpret_cast<const float4 *>(b_st + q * B_STAGE + 2 * B_BYTES) + 4 * q4;
             float hc[4], lc[4], hs[4], ls[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const float c1 = cs[4 * g + e], s1 = sn[4 * g + e];
-                hc[e] = to_tf32(c1);
-                lc[e] = to_tf32(c1 - hc[e]);
-                hs[e] = to_tf32(s1);
-                ls[e] = to_tf32(s1 - hs[e]);
+                const float4 r = p4[e];
+                const float t = __fmaf_rn(kz, r.z, __fmaf_rn(ky, r.y, __fmul_rn(kx, r.x)));
+                float sv, cv;
+                sincos_tc(t, &sv, &cv);
+                hc[e] = to_tf32(cv);
+                lc[e] = to_tf32(cv - hc[e]);
+                hs[e] = to_tf32(sv);
+                ls[e] = to_tf32(sv - hs[e]);
             }
-            const uint32_t off = core_offset(kk, 8 * half + 4 * g);
+            unsigned char *st = a_st + s * A_STAGE;
             *reinterpret_cast<float4 *>(st + 0 * A_BYTES + off) = make_float4(hc[0], hc[1], hc[2], hc[3]);
             *reinterpret_cast<float4 *>(st + 1 * A_BYTES + off) = make_float4(lc[0], lc[1], lc[2], lc[3]);
             *reinterpret_cast<float4 *>(st + 2 * A_BYTES + off) = make_float4(hs[0], hs[1], hs[2], hs[3]);
             *reinterpret_cast<float4 *>(st + 3 * A_BYTES + off) = make_float4(ls[0], ls[1], ls[2], ls[3]);
+            // visible to the tensor cores, then counted
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar_full[s])) : "memory");
         }
-        // the phases are visible to the tensor cores, then one thread issues
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            const int q = c % B_STAGES;
-            if (!mbar_wait(&bar_b[q], (uint32_t)((c / B_STAGES) & 1))) {
+    } else if (lane == 0) { // the issuer
+        int copied = -1, landed = -1, issued = 0;
+        auto copy_chunk = [&](int cc) {
+            const int q = cc % B_STAGES;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b[q])),
+                         "r"(B_STAGE)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_addr(b_st + q * B_STAGE)),
+                "l"(tiles + (int64_t)cc * TILE_FLOATS), "r"(B_STAGE), "r"(smem_addr(&bar_b[q]))
+                : "memory");
+            copied = cc;
+        };
+        for (int cc = 0; cc < B_AHEAD && cc < n_chunks; cc++) copy_chunk(cc);
+        for (int c = 0; c < n_chunks; c++) {
+            const int s = c % A_STAGES, q = c % B_STAGES;
+            bool ok = true;
+            if (c + B_AHEAD < n_chunks) {
+                const int j = c + B_AHEAD - B_STAGES; // the chunk whose buffer the copy reuses
+                if (j >= 0) ok = mbar_wait(&bar_mma[j % A_STAGES], (uint32_t)((j / A_STAGES) & 1));
+                if (ok) copy_chunk(c + B_AHEAD);
+            }
+            ok = ok && mbar_wait(&bar_full[s], (uint32_t)((c / A_STAGES) & 1));
+            ok = ok && mbar_wait(&bar_b[q], (uint32_t)((c / B_STAGES) & 1));
+            if (!ok || *(volatile int *)&s_fail) {
                 s_fail = 1;
-            } else {
-                landed = c;
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t abase = smem_addr(st), bbase = smem_addr(b_st + q * B_STAGE);
+                break;
+            }
+            landed = c;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t abase = smem_addr(a_st + s * A_STAGE), bbase = smem_addr(b_st + q * B_STAGE);
 #pragma unroll
-                for (int j = 0; j < TC_K / 8; j++) { // K-steps of 8 sites: two core-matrix columns
-                    const uint32_t kofs = j * 2 * LBO;
-                    const uint64_t bh = smem_desc(bbase + kofs), bl = smem_desc(bbase + B_BYTES + kofs);
+            for (int j = 0; j < TC_K / 8; j++) { // K-steps of 8 sites: two core-matrix columns
+                const uint32_t kofs = j * 2 * LBO;
+                const uint64_t bh = smem_desc(bbase + kofs), bl = smem_desc(bbase + B_BYTES + kofs);
 #pragma unroll
-                    for (int ph = 0; ph < 2; ph++) { // cos, sin
-                        const uint64_t ah = smem_desc(abase + (2 * ph) * A_BYTES + kofs);
-                        const uint64_t al = smem_desc(abase + (2 * ph + 1) * A_BYTES + kofs);
-                        const uint32_t d = tmem + (ph ? SIN_COL : 0u);
-                        const uint32_t first = (c == 0 && j == 0) ? 0u : 1u; // accumulate after the first
-                        const uint64_t aa[3] = {ah, ah, al}, bb[3] = {bh, bl, bh};
+                for (int ph = 0; ph < 2; ph++) { // cos, sin
+                    const uint64_t ah = smem_desc(abase + (2 * ph) * A_BYTES + kofs);
+                    const uint64_t al = smem_desc(abase + (2 * ph + 1) * A_BYTES + kofs);
+                    const uint32_t d = tmem + (ph ? SIN_COL : 0u);
+                    const uint32_t first = (c == 0 && j == 0) ? 0u : 1u; // accumulate after the first
+                    const uint64_t aa[3] = {ah, ah, al}, bb[3] = {bh, bl, bh};
 #pragma unroll
-                        for (int p = 0; p < 3; p++) {
-                            const uint32_t acc = p == 0 ? first : 1u;
-                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-                                         "l"(aa[p]), "l"(bb[p]), "r"(IDESC), "r"(acc)
-                                         : "memory");
-                        }
+                    for (int p = 0; p < 3; p++) {
+                        const uint32_t acc = p == 0 ? first : 1u;
+                        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                                     "l"(aa[p]), "l"(bb[p]), "r"(IDESC), "r"(acc)
+                                     : "memory");
                     }
                 }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 smem_addr(&bar_mma[s]))
-                             : "memory");
-                issued = c + 1;
             }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&bar_mma[s]))
+                         : "memory");
+            issued = c + 1;
         }
-        if (__syncthreads_or(tid == 0 && s_fail)) break;
-    }
-    // after a failure, the bulk copies still in flight land before the CTA exits
-    if (tid == 0)
+        // after a failure, the copies still in flight land before the CTA exits
         for (int cc = landed + 1; cc <= copied; cc++)
             if (!mbar_wait(&bar_b[cc % B_STAGES], (uint32_t)((cc / B_STAGES) & 1))) break;
-    // wait for the last chunk's MMAs (the commit follows every MMA issued before it)
-    if (tid == 0) s_issued = issued;
+        s_issued = issued;
+    }
     __syncthreads();
+    // the last chunk's MMAs (its commit follows every MMA issued before it)
     const int n_done = s_issued;
     bool ok = !s_fail;
     if (n_done > 0) {
@@ -314,36 +321,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     ok = !__syncthreads_or(!ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok && n_done == n_chunks) {
-        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its wavevectors) for
-        // replicas 32 (w / 4) .. + 31, eight replicas (24 columns) at a time
-        const int lane_base = 32 * (warp & 3), rbase = 32 * (warp >> 2);
-        const int64_t kq = k0 + lane_base + (tid & 31);
-        const double inv_n = 1.0 / (double)n_real;
-        for (int rg = 0; rg < 32; rg += 8) {
-            uint32_t cv[24], sv[24];
-            const uint32_t ta = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(3 * (rbase + rg));
-            tmem_ld8(ta, cv, 0);
-            tmem_ld8(ta + 8, cv, 8);
-            tmem_ld8(ta + 16, cv, 16);
-            tmem_ld8(ta + SIN_COL, sv, 0);
-            tmem_ld8(ta + SIN_COL + 8, sv, 8);
-            tmem_ld8(ta + SIN_COL + 16, sv, 16);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (kq >= n_k) continue;
+        if (producer) {
+            // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its wavevectors) for
+            // replicas 16 (w / 4) .. + 15, eight replicas (24 columns) at a time
+            const int lane_base = 32 * (warp & 3), rbase = 16 * (warp >> 2);
+            const int64_t kq = k0 + lane_base + lane;
+            const double inv_n = 1.0 / (double)n_real;
+            for (int rg = 0; rg < 16; rg += 8) {
+                uint32_t cv[24], sv[24];
+                const uint32_t ta = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(3 * (rbase + rg));
+                tmem_ld8(ta, cv, 0);
+                tmem_ld8(ta + 8, cv, 8);
+                tmem_ld8(ta + 16, cv, 16);
+                tmem_ld8(ta + SIN_COL, sv, 0);
+                tmem_ld8(ta + SIN_COL + 8, sv, 8);
+                tmem_ld8(ta + SIN_COL + 16, sv, 16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (kq >= n_k) continue;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int r = rt * TC_R + rbase + rg + q;
-                if (r >= n_rep) break;
-                const int slot = slot_of[chain_base + r] - slot_base;
-                double *o = out + ((int64_t)slot * n_k + kq) * 9;
+                for (int q = 0; q < 8; q++) {
+                    const int r = rt * TC_R + rbase + rg + q;
+                    if (r >= n_rep) break;
+                    const int slot = slot_of[chain_base + r] - slot_base;
+                    double *o = out + ((int64_t)slot * n_k + kq) * 9;
 #pragma unroll
-                for (int a = 0; a < 3; a++)
+                    for (int a = 0; a < 3; a++)
 #pragma unroll
-                    for (int b = 0; b < 3; b++) {
-                        const double ca = __uint_as_float(cv[3 * q + a]), cb = __uint_as_float(cv[3 * q + b]);
-                        const double sa = __uint_as_float(sv[3 * q + a]), sb = __uint_as_float(sv[3 * q + b]);
-                        o[3 * a + b] = (ca * cb + sa * sb) * inv_n;
-                    }
+                        for (int b = 0; b < 3; b++) {
+                            const double ca = __uint_as_float(cv[3 * q + a]), cb = __uint_as_float(cv[3 * q + b]);
+                            const double sa = __uint_as_float(sv[3 * q + a]), sb = __uint_as_float(sv[3 * q + b]);
+                            o[3 * a + b] = (ca * cb + sa * sb) * inv_n;
+                        }
+                }
             }
         }
     } else if (tid == 0) {
@@ -357,7 +366,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 int64_t sf_tc_sites(int64_t Np) { return (Np + TC_K - 1) / TC_K * TC_K; }
 int64_t sf_tc_packed_floats(int64_t Np, int n_rep) {
-    return (int64_t)((n_rep + TC_R - 1) / TC_R) * (sf_tc_sites(Np) / TC_K) * 2 * TC_N * TC_K;
+    return (int64_t)((n_rep + TC_R - 1) / TC_R) * (sf_tc_sites(Np) / TC_K) * TILE_FLOATS;
 }
 
 cudaError_t launch_structure_factor_tc(const SysArgs<float> &a, const float *pos, const float *ks, int64_t n_k,
@@ -368,13 +377,13 @@ cudaError_t launch_structure_factor_tc(const SysArgs<float> &a, const float *pos
     const int64_t n_chunks = sf_tc_sites(a.tb.Np) / TC_K;
     if (n_chunks * TC_N * TC_K > (int64_t)INT32_MAX) return cudaErrorInvalidValue;
     const int64_t per_tile = n_chunks * TC_N * TC_K;
-    k_sf_pack<<<dim3((unsigned)((per_tile + 255) / 256), (unsigned)n_rt), 256, 0, st>>>(a.spins, a.tb.Np, a.n_rep,
-                                                                                      (int)n_chunks, packed);
+    k_sf_pack<<<dim3((unsigned)((per_tile + 255) / 256), (unsigned)n_rt), 256, 0, st>>>(a.spins, pos, a.tb.Np,
+                                                                                      a.n_rep, (int)n_chunks, packed);
     cudaError_t e = cudaFuncSetAttribute((const void *)k_structure_factor_tc,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess) return e;
     const dim3 grid((unsigned)((n_k + TC_M - 1) / TC_M), (unsigned)n_rt);
-    k_structure_factor_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(packed, (int)n_chunks, a.n_rep, pos, ks, n_k, a.n_real,
+    k_structure_factor_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(packed, (int)n_chunks, a.n_rep, ks, n_k, a.n_real,
                                                              slot_of, a.chain_base, slot_base, out, error_flag);
     return cudaGetLastError();
 }
