@@ -469,13 +469,16 @@ def bench_structure_factor(args):
     """compute_equal_time_correlations of all 64 replicas of the simple-cubic
     L=24 workload at every allowed wavevector 2 pi n / L (13824 k-points),
     FP32: site-phase products (k-points x sites x replicas) per second of
-    device time."""
+    device time.  `--cuda-cores` times the CUDA-core kernel instead of the
+    tensor-core one (csmc_set_tensor_cores)."""
     import torch
     m = G.load()
     torch.cuda.set_device(0)
     lat = make_lattice(m)
     mc = m.MonteCarlo(list(temperatures()), lat, {}, precision="fp32", seed=SEED)
     mc.ctx.call("csmc_random_spins", C.c_uint64(SEED))
+    if args.cuda_cores:
+        mc.ctx.call("csmc_set_tensor_cores", 0)
     n = np.stack(np.unravel_index(np.arange(L_SIDE ** 3), (L_SIDE,) * 3), axis=0)
     ks = np.asfortranarray(2 * np.pi * n / L_SIDE, dtype=np.float64)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -488,15 +491,37 @@ def bench_structure_factor(args):
             torch.cuda.synchronize()
             m.structure_factors(mc, ks)
             t += stats(mc.ctx)[0] / 1e3
-    products = ks.shape[1] * lat.size * R_REPL
+    n_k, N = ks.shape[1], lat.size
+    products = n_k * N * R_REPL
     line = {"metric": "structure factor: k-point x site x replica products per second", "value": products * args.steps / t,
             "unit": "products/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "structure_factor", "lattice": "simple cubic L=24 (13824 sites)",
-                       "replicas": R_REPL, "k_points": int(ks.shape[1]),
-                       "fp32_fma_per_product": 6, "l2": "flushed between steps (256 MB write)"},
-            "clocks": clk.summary(), "gpu_launches": args.steps}
+                       "replicas": R_REPL, "k_points": int(n_k),
+                       "kernel": "CUDA cores (6 FP32 FMA per product)" if args.cuda_cores else
+                                 "tensor cores (tcgen05 TF32, operands split hi+lo, 3 products)",
+                       "l2": "flushed between steps (256 MB write)"},
+            "clocks": clk.summary(), "gpu_launches": args.steps * (1 if args.cuda_cores else 2)}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    if args.cuda_cores:
+        flop = 12.0 * products  # 6 FMA per product
+        peak = 152 * 128 * 2 * (clk.summary().get("sm_mhz") or 2070.0) * 1e6 / 1e12  # FP32 FMA, sampled clock
+        line["roofline"] = {"bound": "fp32", "achieved": flop * args.steps / t / 1e12, "peak": peak,
+                            "unit": "TFLOP/s", "frac": flop * args.steps / t / 1e12 / peak, "traffic": None,
+                            "peak_source": "nominal 152 SMs x 128 FP32 FMA/clk at the sampled clock"}
+    else:
+        # the MMAs' work: cos and sin, three split products, 2 FLOP per MAC, over
+        # the padded sites (multiple of 16) and 192 spin columns per 64 replicas
+        n_pad = -(-N // 16) * 16
+        flop = 3 * 2 * 2.0 * n_k * n_pad * 3 * (-(-R_REPL // 64) * 64)
+        peak = peaks.get("bf16_tflops", 1900.0) / 2  # TF32 runs at half the bf16 rate
+        line["roofline"] = {"bound": "tensor", "achieved": flop * args.steps / t / 1e12, "peak": peak,
+                            "unit": "TFLOP/s", "frac": flop * args.steps / t / 1e12 / peak, "traffic": None,
+                            "peak_source": "TF32 = half of MEASURED_PEAKS.json bf16_tflops (measured cuBLAS bf16)",
+                            "note": "time includes the spin-packing launch; 108 tiles of 128 wavevectors x "
+                                    "64 replicas, sites split 7 ways (756 CTAs on 152 SMs), the last CTA of a "
+                                    "tile adding its partial sums"}
     print(json.dumps(line))
 
 
@@ -514,6 +539,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="skip csmc_autotune (library heuristics)")
     ap.add_argument("--path", default="auto", choices=["auto", "resident", "global"],
                     help="execution path of csmc_run (auto: the autotuner's choice)")
+    ap.add_argument("--cuda-cores", action="store_true",
+                    help="structure_factor workload: the CUDA-core kernel instead of the tensor cores")
     ap.add_argument("--no-persistent", action="store_true",
                     help="one launch per exchange window (csmc_set_persistent 0), e.g. under a profiler")
     ap.add_argument("--workload", default="sc_pt",

@@ -63,6 +63,10 @@ template <typename T> struct DevBuf {
         if (count) CK(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
     }
     template <class V> void upload(const V &v) { upload(v.data(), v.size()); }
+    // at least `count` elements, reallocating only to grow (contents not kept)
+    void reserve(size_t count) {
+        if (count > n) alloc(count);
+    }
     void zero(cudaStream_t st) {
         if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
     }
@@ -157,6 +161,7 @@ struct Ctx {
     std::vector<std::unique_ptr<Group>> groups; // one, or the size groups
     bool size_groups = false;                   // csmc_set_size_groups / the autotuner's choice
     bool sf_tensor = true; // single-precision structure factors on the tensor cores (csmc_set_tensor_cores)
+    DevBuf<float> sf_packed, sf_partial; // their scratch (split spins, partial sums), kept and grown
     int group_block_cap = 0; // size groups: at most this many threads per CTA (0: none), so CTAs of
                              // several groups share an SM (the autotuner's choice)
     cudaEvent_t fork = nullptr;                 // size groups start after the work queued before them
@@ -1384,16 +1389,18 @@ static void structure_factor(Ctx &C, System &S, const SysArgs<R> &a, int dim, co
     dpos.upload(pd);
     dks.upload(kd);
     dout.alloc((size_t)S.R * std::max<int64_t>(n_k, 1) * 9);
+    const int splits = tensor ? sf_tc_splits(n_k, S.R, P.Np, C.n_sms) : 1;
+    if (tensor) {
+        C.sf_packed.reserve((size_t)sf_tc_packed_floats(P.Np, S.R));
+        C.sf_partial.reserve((size_t)sf_tc_partial_floats(n_k, S.R, splits));
+    }
     C.reset_kernel_time();
     auto ev = C.next_kernel_events();
     CK(cudaEventRecord(ev.first, C.st));
-    DevBuf<float> packed;
     if constexpr (sizeof(R) == 4) {
-        if (tensor) {
-            packed.alloc((size_t)sf_tc_packed_floats(P.Np, S.R));
-            CK(launch_structure_factor_tc(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, packed.p,
-                                          C.error_flag.p, C.st));
-        }
+        if (tensor)
+            CK(launch_structure_factor_tc(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, C.sf_packed.p,
+                                          C.sf_partial.p, splits, C.error_flag.p, C.st));
     }
     if (!tensor) launch_structure_factor<R>(a, dpos.p, dks.p, n_k, C.slot_of.p, S.base, dout.p, C.st);
     CK(cudaEventRecord(ev.second, C.st));

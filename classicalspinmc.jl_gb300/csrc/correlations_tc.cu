@@ -14,16 +14,19 @@
 // replica-major, x y z), the sites in chunks of 16 (two MMA K-steps of 8).
 // Warp-specialised pipeline, synchronised by mbarriers only:
 //  * 16 producer warps evaluate each chunk's 128 x 16 phases (range-reduced
-//    hardware sincos) and store their TF32 halves in shared memory in the
+//    hardware sincos; the sites' positions read from the packed tiles one
+//    chunk ahead) and store their TF32 halves in shared memory in the
 //    no-swizzle K-major core-matrix layout (three phase stages; a quarter-warp
 //    writes one 128-byte core-matrix column, so the stores are conflict-free);
 //  * one issuer warp brings each chunk's spins -- split and laid out the same
-//    way beforehand by k_sf_pack, one layout for every wavevector tile -- and
-//    the chunk's site positions by one bulk copy two chunks ahead (four
-//    buffers), and, once the chunk's phases are written, issues its 12 MMAs
-//    (cos and sin, three products, two K-steps) and commits them.
+//    way beforehand by k_sf_pack, one layout for every wavevector tile -- by
+//    one bulk copy three chunks ahead (five buffers), and, once the chunk's
+//    phases are written, issues its 12 MMAs (cos and sin, three products, two
+//    K-steps) and commits them.
 // The accumulators (cos sums in TMEM columns 0..191, sin sums in 256..447)
-// are read back with tcgen05.ld and turned into the nine products in FP64.
+// are read back with tcgen05.ld and turned into the nine products in FP32,
+// stored as doubles.  When there are fewer tiles than SMs, a tile's sites are
+// split over several CTAs whose partial sums the last of them adds up.
 //
 // Every wait is bounded (one second of %globaltimer): on a timeout the CTA
 // sets the error flag, waits (bounded) for the copies and the MMAs it issued,
@@ -48,10 +51,18 @@ constexpr uint32_t A_STAGE = 4 * A_BYTES;          // cos hi|lo, sin hi|lo of on
 constexpr uint32_t B_STAGE = 2 * B_BYTES + POS_BYTES; // spins hi|lo and positions of one chunk
 constexpr int TILE_FLOATS = (int)(B_STAGE / 4);    // one chunk of k_sf_pack's output
 constexpr int A_STAGES = 3;
-constexpr int B_STAGES = 4;
-constexpr int B_AHEAD = 2; // a chunk's copy is issued while the MMAs of the chunk two before it run
-constexpr uint32_t TC_SMEM = A_STAGES * A_STAGE + B_STAGES * B_STAGE; // 193 KB: one CTA per SM, which
-                                                                      // takes all 512 TMEM columns
+constexpr int B_STAGES = 5;
+constexpr int B_AHEAD = 3; // a chunk's spins are copied three chunks before its MMAs are issued
+constexpr uint32_t PIPE_SMEM = A_STAGES * A_STAGE + B_STAGES * B_STAGE; // 217 KB
+// the epilogue's stage of the sums, [384 columns][SPAD] floats over the
+// pipeline's buffers: a column of 128 wavevectors padded to 132 floats, so
+// that the three components of a replica (columns 3r .. 3r + 2) of one
+// wavevector fall in different banks
+constexpr int SPAD = TC_M + 4;
+constexpr uint32_t STAGE_SMEM = 2 * TC_N * SPAD * 4; // 198 KB
+constexpr uint32_t TC_SMEM = PIPE_SMEM > STAGE_SMEM ? PIPE_SMEM : STAGE_SMEM; // one CTA per SM, which
+                                                                             // takes all 512 TMEM columns
+static_assert(TC_SMEM <= 227 * 1024, "shared memory of one CTA");
 // the copy of chunk c + B_AHEAD reuses the buffer of chunk c + B_AHEAD - B_STAGES,
 // whose MMAs the issuer waits for; that chunk must precede c
 static_assert(B_STAGES > B_AHEAD, "a spin buffer is refilled only after the MMAs that read it");
@@ -108,8 +119,10 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
                  : "memory");
     return ok != 0;
 }
-// bounded wait for phase `parity` of an mbarrier; false on timeout
+// bounded wait for phase `parity` of an mbarrier; false on timeout (the
+// timer is read only once the phase is found incomplete)
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    if (mbar_test(bar, parity)) return true;
     const uint64_t t0 = gtimer();
     do {
         if (mbar_test(bar, parity)) return true;
@@ -165,19 +178,44 @@ __global__ void k_sf_pack(const float *__restrict__ spins, const float *__restri
             make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
 }
 
-// ks: 3 per wavevector; packed: k_sf_pack's tiles; out[slot][k][9].
+// A float widened to double with integer operations (sign kept, exponent
+// rebiased by 1023 - 127, mantissa shifted up by 29 bits; infinities and NaNs
+// kept; the rare subnormal float becomes a signed zero).  This GPU's FP64
+// pipe runs at a small fraction of its FP32 rate, and the epilogue writes
+// nine doubles per (wavevector, replica): the conversions stay off it.
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xFFu;
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    if (e == 0u) return __longlong_as_double((long long)sign);
+    const uint64_t ex = e == 0xFFu ? 0x7FFull : (uint64_t)(e + 896u);
+    return __longlong_as_double((long long)(sign | (ex << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
+}
+
+// ks: 3 per wavevector; packed: k_sf_pack's tiles; out[slot][k][9].  Grid:
+// (splits x wavevector tiles, replica tiles), the split fastest so that a
+// tile's CTAs run together.  The sites of a tile are split
+// over `splits` CTAs of split_chunks chunks each: with one split the CTA forms
+// the products itself; with several, each writes its partial cos and sin sums
+// to `partial` ([tile][split][384 columns][128 rows], FP32), and the last of
+// the tile's CTAs to finish (counted in tile_ctr, zero before the launch)
+// forms the products from all of them.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_structure_factor_tc(const float *__restrict__ packed, int n_chunks, int n_rep, const float *__restrict__ ks,
-                          int64_t n_k, int64_t n_real, const int32_t *__restrict__ slot_of, int chain_base,
-                          int slot_base, double *__restrict__ out, int *error_flag) {
+    k_structure_factor_tc(const float *__restrict__ packed, int n_chunks, int split_chunks, int n_rep,
+                          const float *__restrict__ ks, int64_t n_k, float inv_n,
+                          const int32_t *__restrict__ slot_of, int chain_base, int slot_base,
+                          double *__restrict__ out, float *__restrict__ partial, int *__restrict__ tile_ctr,
+                          int splits, int *error_flag) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t bar_b[B_STAGES], bar_full[A_STAGES], bar_mma[A_STAGES];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_fail, s_issued;
+    __shared__ int s_fail, s_issued, s_last;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool producer = tid < TC_PRODUCERS;
-    const int64_t k0 = (int64_t)blockIdx.x * TC_M;
+    const int split = (int)(blockIdx.x % splits), kt = (int)(blockIdx.x / splits);
+    const int64_t k0 = (int64_t)kt * TC_M;
     const int rt = blockIdx.y;
+    const int64_t tile = (int64_t)rt * (gridDim.x / splits) + kt;
+    float *const tile_partial = partial ? partial + tile * splits * (2 * TC_N) * TC_M : nullptr;
     unsigned char *const a_st = smem;                       // A_STAGES x (cos hi, cos lo, sin hi, sin lo)
     unsigned char *const b_st = smem + A_STAGES * A_STAGE; // B_STAGES x (spins hi, spins lo, positions)
 
@@ -201,7 +239,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
-    const float *tiles = packed + (int64_t)rt * n_chunks * TILE_FLOATS;
+    // this CTA's chunks: [c_begin, c_begin + n_my); loop indices below count from c_begin
+    const int c_begin = split * split_chunks;
+    const int n_my = max(0, min(n_chunks, c_begin + split_chunks) - c_begin);
+    const float *tiles = packed + ((int64_t)rt * n_chunks + c_begin) * TILE_FLOATS;
 
     if (producer) {
         // row (wavevector) and core-matrix column (4 sites) of this thread: a
@@ -215,20 +256,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             kz = ks[3 * k + 2];
         }
         const uint32_t off = core_offset(row, 4 * q4);
-        for (int c = 0; c < n_chunks; c++) {
-            const int s = c % A_STAGES, q = c % B_STAGES;
-            bool ok = mbar_wait(&bar_b[q], (uint32_t)((c / B_STAGES) & 1)); // the chunk's positions
-            if (ok && c >= A_STAGES) // the MMAs of chunk c - A_STAGES have read this phase stage
+        // this thread's four site positions of a chunk, read from the packed
+        // tiles (L2) one chunk ahead, so the phases never wait for the spins' copy
+        auto positions = [&](int c, float4 (&p)[4]) {
+            const float4 *g = reinterpret_cast<const float4 *>(tiles + (int64_t)c * TILE_FLOATS + 2 * TC_N * TC_K);
+#pragma unroll
+            for (int e = 0; e < 4; e++) p[e] = __ldg(g + 4 * q4 + e);
+        };
+        float4 pn[4];
+        if (n_my > 0) positions(0, pn);
+        for (int c = 0; c < n_my; c++) {
+            const int s = c % A_STAGES;
+            float4 pc[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) pc[e] = pn[e];
+            if (c + 1 < n_my) positions(c + 1, pn);
+            bool ok = true;
+            if (c >= A_STAGES) // the MMAs of chunk c - A_STAGES have read this phase stage
                 ok = mbar_wait(&bar_mma[s], (uint32_t)(((c - A_STAGES) / A_STAGES) & 1));
             if (!ok || *(volatile int *)&s_fail) {
                 s_fail = 1;
                 break;
             }
-            const float4 *p4 = reinterpret_cast<const float4 *>(b_st + q * B_STAGE + 2 * B_BYTES) + 4 * q4;
             float hc[4], lc[4], hs[4], ls[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const float4 r = p4[e];
+                const float4 r = pc[e];
                 const float t = __fmaf_rn(kz, r.z, __fmaf_rn(ky, r.y, __fmul_rn(kx, r.x)));
                 float sv, cv;
                 sincos_tc(t, &sv, &cv);
@@ -260,11 +313,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 : "memory");
             copied = cc;
         };
-        for (int cc = 0; cc < B_AHEAD && cc < n_chunks; cc++) copy_chunk(cc);
-        for (int c = 0; c < n_chunks; c++) {
+        for (int cc = 0; cc < B_AHEAD && cc < n_my; cc++) copy_chunk(cc);
+        for (int c = 0; c < n_my; c++) {
             const int s = c % A_STAGES, q = c % B_STAGES;
             bool ok = true;
-            if (c + B_AHEAD < n_chunks) {
+            if (c + B_AHEAD < n_my) {
                 const int j = c + B_AHEAD - B_STAGES; // the chunk whose buffer the copy reuses
                 if (j >= 0) ok = mbar_wait(&bar_mma[j % A_STAGES], (uint32_t)((j / A_STAGES) & 1));
                 if (ok) copy_chunk(c + B_AHEAD);
@@ -320,71 +373,148 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     ok = !__syncthreads_or(!ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && n_done == n_chunks) {
-        if (producer) {
-            // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its wavevectors) for
-            // replicas 16 (w / 4) .. + 15, eight replicas (24 columns) at a time
-            const int lane_base = 32 * (warp & 3), rbase = 16 * (warp >> 2);
-            const int64_t kq = k0 + lane_base + lane;
-            const double inv_n = 1.0 / (double)n_real;
-            for (int rg = 0; rg < 16; rg += 8) {
-                uint32_t cv[24], sv[24];
-                const uint32_t ta = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(3 * (rbase + rg));
-                tmem_ld8(ta, cv, 0);
-                tmem_ld8(ta + 8, cv, 8);
-                tmem_ld8(ta + 16, cv, 16);
-                tmem_ld8(ta + SIN_COL, sv, 0);
-                tmem_ld8(ta + SIN_COL + 8, sv, 8);
-                tmem_ld8(ta + SIN_COL + 16, sv, 16);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (kq >= n_k) continue;
+    // The sums of this CTA's sites, TMEM -> the stage in shared memory (the
+    // pipeline's buffers, idle now: every copy has landed and every MMA that
+    // read them has completed): [384 columns: cos x y z of replica 0 .. 63,
+    // then sin][SPAD], FP32.  Warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
+    // wavevectors) for replicas 16 (w / 4) .. + 15.
+    float *const stage = reinterpret_cast<float *>(smem);
+    const bool have = ok && n_done == n_my && n_my > 0;
+    if (have && producer) {
+        const int lane_base = 32 * (warp & 3), rbase = 16 * (warp >> 2), row = lane_base + lane;
+        for (int rg = 0; rg < 16; rg += 8) {
+            uint32_t cv[24], sv[24];
+            const uint32_t col = (uint32_t)(3 * (rbase + rg));
+            const uint32_t ta = tmem + ((uint32_t)lane_base << 16) + col;
+            tmem_ld8(ta, cv, 0);
+            tmem_ld8(ta + 8, cv, 8);
+            tmem_ld8(ta + 16, cv, 16);
+            tmem_ld8(ta + SIN_COL, sv, 0);
+            tmem_ld8(ta + SIN_COL + 8, sv, 8);
+            tmem_ld8(ta + SIN_COL + 16, sv, 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    const int r = rt * TC_R + rbase + rg + q;
-                    if (r >= n_rep) break;
-                    const int slot = slot_of[chain_base + r] - slot_base;
-                    double *o = out + ((int64_t)slot * n_k + kq) * 9;
-#pragma unroll
-                    for (int a = 0; a < 3; a++)
-#pragma unroll
-                        for (int b = 0; b < 3; b++) {
-                            const double ca = __uint_as_float(cv[3 * q + a]), cb = __uint_as_float(cv[3 * q + b]);
-                            const double sa = __uint_as_float(sv[3 * q + a]), sb = __uint_as_float(sv[3 * q + b]);
-                            o[3 * a + b] = (ca * cb + sa * sb) * inv_n;
-                        }
-                }
+            for (int e = 0; e < 24; e++) {
+                stage[(col + e) * SPAD + row] = __uint_as_float(cv[e]);
+                stage[(TC_N + col + e) * SPAD + row] = __uint_as_float(sv[e]);
             }
         }
-    } else if (tid == 0) {
-        atomicExch(error_flag, 1);
     }
+    if (!have && tid == 0) atomicExch(error_flag, 1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    if (!have) return; // block-uniform
+    // float4 i of a split's partial sums ([384][128] in global memory): column
+    // i / 32, wavevectors 4 (i % 32) .. + 3; in the stage at column * SPAD / 4
+    constexpr int STAGE4 = 2 * TC_N * TC_M / 4, Q4 = TC_M / 4, SPAD4 = SPAD / 4;
+    float4 *const stage4 = reinterpret_cast<float4 *>(stage);
+    if (splits > 1) {
+        // this split's sums to the tile's partial buffer, then counted; the
+        // last CTA of the tile to finish adds every split's sums, in split
+        // order (the same result whichever CTA that is), into its stage
+        float4 *const mine = reinterpret_cast<float4 *>(tile_partial) + (int64_t)split * STAGE4;
+        for (int i = tid; i < STAGE4; i += blockDim.x) __stcg(mine + i, stage4[(i / Q4) * SPAD4 + i % Q4]);
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(&tile_ctr[tile], 1) == splits - 1;
+        __syncthreads();
+        if (!s_last) return; // block-uniform
+        __threadfence();
+        const float4 *const all = reinterpret_cast<const float4 *>(tile_partial);
+        for (int i = tid; i < STAGE4; i += blockDim.x) {
+            float4 *const dst = stage4 + (i / Q4) * SPAD4 + i % Q4;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int z = 0; z < splits; z++) {
+                const float4 v = z == split ? *dst : __ldcg(all + (int64_t)z * STAGE4 + i);
+                acc.x = __fadd_rn(acc.x, v.x);
+                acc.y = __fadd_rn(acc.y, v.y);
+                acc.z = __fadd_rn(acc.z, v.z);
+                acc.w = __fadd_rn(acc.w, v.w);
+            }
+            *dst = acc;
+        }
+        __syncthreads();
+    }
+    // Suv[3a+b] = (C_a C_b + S_a S_b) / N in FP32 (the sums carry FP32
+    // accuracy already), stored as doubles.  A replica's 9 x (valid
+    // wavevectors) outputs are contiguous: consecutive threads write
+    // consecutive doubles.
+    const int rows = (int)min((int64_t)TC_M, n_k - k0);
+    for (int rl = 0; rl < TC_R; rl++) {
+        const int r = rt * TC_R + rl;
+        if (r >= n_rep) break;
+        double *const o = out + ((int64_t)(slot_of[chain_base + r] - slot_base) * n_k + k0) * 9;
+        for (int j = tid; j < 9 * rows; j += blockDim.x) {
+            const int row = j / 9, e = j - 9 * row, a = e / 3, b = e - 3 * a;
+            const float ca = stage[(3 * rl + a) * SPAD + row], cb = stage[(3 * rl + b) * SPAD + row];
+            const float sa = stage[(TC_N + 3 * rl + a) * SPAD + row], sb = stage[(TC_N + 3 * rl + b) * SPAD + row];
+            o[j] = widen(__fmul_rn(__fmaf_rn(ca, cb, __fmul_rn(sa, sb)), inv_n));
+        }
+    }
 }
 
+
 int64_t sf_tc_sites(int64_t Np) { return (Np + TC_K - 1) / TC_K * TC_K; }
+
+// Splits of the sites per tile: the number s <= 8 (and <= the chunks) that
+// minimises the launch's waves per unit of work, ceil(tiles s / SMs) / s
+// (one CTA per SM); ties go to the smaller s.
+int sf_tc_splits(int64_t n_k, int n_rep, int64_t Np, int n_sms) {
+    const int64_t tiles = ((n_k + TC_M - 1) / TC_M) * ((n_rep + TC_R - 1) / TC_R);
+    const int64_t chunks = sf_tc_sites(Np) / TC_K;
+    int best = 1;
+    double best_cost = 1e300;
+    for (int s = 1; s <= 8 && s <= chunks; s++) {
+        const double cost = (double)((tiles * s + n_sms - 1) / n_sms) / s;
+        if (cost < best_cost - 1e-12) {
+            best_cost = cost;
+            best = s;
+        }
+    }
+    return best;
+}
+// the partial sums and (after them, 16-byte aligned) the per-tile counters
+int64_t sf_tc_partial_floats(int64_t n_k, int n_rep, int splits) {
+    if (splits <= 1) return 0;
+    const int64_t tiles = ((n_k + TC_M - 1) / TC_M) * ((n_rep + TC_R - 1) / TC_R);
+    return (int64_t)splits * tiles * (2 * TC_N) * TC_M + (tiles + 3) / 4 * 4;
+}
 int64_t sf_tc_packed_floats(int64_t Np, int n_rep) {
     return (int64_t)((n_rep + TC_R - 1) / TC_R) * (sf_tc_sites(Np) / TC_K) * TILE_FLOATS;
 }
 
 cudaError_t launch_structure_factor_tc(const SysArgs<float> &a, const float *pos, const float *ks, int64_t n_k,
                                        const int32_t *slot_of, int slot_base, double *out, float *packed,
-                                       int *error_flag, cudaStream_t st) {
+                                       float *partial, int splits, int *error_flag, cudaStream_t st) {
     if (n_k <= 0) return cudaSuccess;
     const int n_rt = (a.n_rep + TC_R - 1) / TC_R;
+    const int64_t n_kt = (n_k + TC_M - 1) / TC_M;
     const int64_t n_chunks = sf_tc_sites(a.tb.Np) / TC_K;
-    if (n_chunks * TC_N * TC_K > (int64_t)INT32_MAX) return cudaErrorInvalidValue;
+    if (n_chunks < 1 || n_chunks * TC_N * TC_K > (int64_t)INT32_MAX || splits < 1 || (splits > 1 && !partial) ||
+        (int64_t)splits * n_kt > (int64_t)INT32_MAX || n_rt > 65535)
+        return cudaErrorInvalidValue;
+    // every split gets at least one chunk (the buffer sized for `splits` covers the rest)
+    const int split_chunks = (int)((n_chunks + splits - 1) / splits);
+    splits = (int)((n_chunks + split_chunks - 1) / split_chunks);
     const int64_t per_tile = n_chunks * TC_N * TC_K;
     k_sf_pack<<<dim3((unsigned)((per_tile + 255) / 256), (unsigned)n_rt), 256, 0, st>>>(a.spins, pos, a.tb.Np,
                                                                                       a.n_rep, (int)n_chunks, packed);
     cudaError_t e = cudaFuncSetAttribute((const void *)k_structure_factor_tc,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess) return e;
-    const dim3 grid((unsigned)((n_k + TC_M - 1) / TC_M), (unsigned)n_rt);
-    k_structure_factor_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(packed, (int)n_chunks, a.n_rep, ks, n_k, a.n_real,
-                                                             slot_of, a.chain_base, slot_base, out, error_flag);
+    int *tile_ctr = nullptr;
+    if (splits > 1) {
+        tile_ctr = reinterpret_cast<int *>(partial + (int64_t)splits * n_kt * n_rt * (2 * TC_N) * TC_M);
+        e = cudaMemsetAsync(tile_ctr, 0, sizeof(int) * (size_t)n_kt * n_rt, st);
+        if (e != cudaSuccess) return e;
+    }
+    const dim3 grid((unsigned)(splits * n_kt), (unsigned)n_rt);
+    k_structure_factor_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(packed, (int)n_chunks, split_chunks, a.n_rep, ks, n_k,
+                                                             (float)(1.0 / (double)a.n_real), slot_of, a.chain_base, slot_base, out,
+                                                             splits > 1 ? partial : nullptr, tile_ctr, splits,
+                                                             error_flag);
     return cudaGetLastError();
 }
 

@@ -69,11 +69,15 @@ void launch_philox(const uint32_t *ctr, const uint32_t *key, int64_t n, uint32_t
 // the same on the tensor cores for a single-precision lattice (correlations_tc.cu):
 // pos 3 per device site for sf_tc_sites(Np) sites (zero-padded), packed
 // sf_tc_packed_floats(Np, n_rep) floats of scratch for the split spins
+// scratch for the split spins, and (splits > 1: the sites of a tile split over
+// several CTAs to fill the SMs) sf_tc_partial_floats of partial sums
 int64_t sf_tc_sites(int64_t Np);
 int64_t sf_tc_packed_floats(int64_t Np, int n_rep);
+int sf_tc_splits(int64_t n_k, int n_rep, int64_t Np, int n_sms);
+int64_t sf_tc_partial_floats(int64_t n_k, int n_rep, int splits);
 cudaError_t launch_structure_factor_tc(const SysArgs<float> &a, const float *pos, const float *ks, int64_t n_k,
                                        const int32_t *slot_of, int slot_base, double *out, float *packed,
-                                       int *error_flag, cudaStream_t st);
+                                       float *partial, int splits, int *error_flag, cudaStream_t st);
 // a kernel whose bounded wait cannot complete (see csmc_selftest_timeout)
 cudaError_t launch_wait_selftest(int which, unsigned int *ctr, int *error_flag, cudaStream_t st);
 // static shared memory of the selected resident kernel in bytes (-1: query failed)

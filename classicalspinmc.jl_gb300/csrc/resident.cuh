@@ -89,6 +89,7 @@ constexpr uint64_t WAIT_BUDGET_NS = 1000000000ull; // one second
 // reports it through the context's error flag instead of hanging.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *error_flag,
                                                   uint64_t budget = WAIT_BUDGET_NS) {
+    if (mbar_try_wait(bar, parity)) return true; // the timer is read only for a phase still open
     const uint64_t t0 = gtimer_ns();
     do {
         if (mbar_try_wait(bar, parity)) return true;
@@ -111,14 +112,16 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *ctr, unsigned int n_b
         atomicAdd(ctr, 1u);
         const unsigned int target = epoch * n_blocks;
         int ok = 0;
-        const uint64_t t0 = gtimer_ns();
-        for (int k = 0; gtimer_ns() - t0 < budget; k++) {
+        uint64_t t0 = 0;
+        for (int k = 0;; k++) {
             unsigned int v;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
             if (v >= target) {
                 ok = 1;
                 break;
             }
+            if (k == 0) t0 = gtimer_ns(); // the timer is read only once the barrier is found open
+            else if (gtimer_ns() - t0 >= budget) break;
             if ((k & 63) == 63 && *(volatile int *)error_flag) break;
             __nanosleep(64);
         }

@@ -344,8 +344,13 @@ int csmc_size_groups(void *ctx, int32_t *n_groups);
  * contiguous, reference site order); ks: dim x n_k column-major; Suv:
  * [replicas of the lattice][n_k][9], the reference's 9 x N_k array per slot
  * in slot order.  Computed in the context's precision (sums of the phases
- * times the spins), the products of the sums in Float64.  csmc_last_run_stats
- * reports the kernel's device time. */
+ * times the spins), the products of the sums in Float64 -- on the tensor
+ * cores (csmc_set_tensor_cores) in FP32, the precision of the sums, and
+ * returned as Float64.  The tensor-core path keeps its device scratch with
+ * the context, grown as needed: the split spins, and partial sums (192 KB per
+ * tile of 128 wavevectors x 64 replicas and per CTA its sites are split over,
+ * when there are fewer tiles than SMs).  csmc_last_run_stats reports the
+ * kernels' device time. */
 int csmc_structure_factor(void *ctx, int32_t lattice, int32_t dim, const double *positions, int64_t n_k,
                           const double *ks, double *Suv);
 

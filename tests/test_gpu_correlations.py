@@ -111,13 +111,17 @@ def test_parallel_tempering_saves_initial_configurations(m, orc):
 
 @pytest.mark.parametrize("name,shape,R,n_k,aligned", [("sc", (4, 4, 4), 17, 77, False), ("sc", (6, 6, 6), 70, 130, False),
                                                        ("square", (8, 8), 3, 200, False), ("sc", (6, 6, 6), 5, 40, True),
-                                                       ("pyrochlore", (2, 2, 3), 1, 129, False)])
+                                                       ("pyrochlore", (2, 2, 3), 1, 129, False),
+                                                       ("sc", (4, 4, 4), 1, 19456, False)])
 def test_tensor_core_structure_factor(m, orc, name, shape, R, n_k, aligned):
     """Single precision on the tensor cores (tcgen05, each operand split into
     two TF32 halves) against the oracle and against the CUDA-core kernel, with
     the FP32 tolerance 2e-5 x N: wavevector counts that are not multiples of
     the 128-wavevector tile, more than 64 replicas (two replica tiles), and all
-    spins aligned (|S(0)|^2 / N = N, the largest sums)."""
+    spins aligned (|S(0)|^2 / N = N, the largest sums).  The sites of a tile
+    are split over several CTAs when there are fewer tiles than SMs (4 splits
+    of 1 chunk at 64 sites; 8 asked for 14 chunks, 7 run), and not at 152
+    tiles (19456 wavevectors)."""
     E = m.examples
     uc = {"square": E.square_heisenberg, "sc": E.sc_heisenberg, "pyrochlore": E.pyrochlore_ckq}[name]()
     lat = m.Lattice(shape, uc, 1.0)
