@@ -796,19 +796,18 @@ static const double *device_view(const void *host) {
     return static_cast<const double *>(at.devicePointer);
 }
 
-// Slots [first, first+n) of one lattice from / to the FP64 reference layout:
-// one bulk copy between the host buffer and the device staging buffer and one
-// conversion launch.  A small pinned buffer (below kDirectBytes) is read or
-// written by the conversion kernel in place instead: one launch, no copy; a
-// large one moves faster as one bulk copy (the kernel's scattered accesses
-// would cross the host link element by element).  Returns after the host
-// buffer has been read (set) or written (get).
-constexpr size_t kDirectBytes = (size_t)1 << 20;
+// Slots [first, first+n) of one lattice from / to the FP64 reference layout.
+// A host buffer the device can address (pinned or registered host memory)
+// is read or written in place by the conversion kernel, whose
+// accesses of it are consecutive (two doubles per thread where aligned): one
+// launch at the host link's rate, no staging copy.  Pageable host memory goes
+// through one bulk copy to or from the device staging buffer and the same
+// launch.  Returns after the host buffer has been read (set) or written (get).
 
 static void set_spins_range(Ctx &C, System &S, int first, int n, const double *host) {
     if (n <= 0) return;
     const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
-    const double *src = bytes < kDirectBytes ? device_view(host) : nullptr;
+    const double *src = device_view(host);
     if (!src) {
         CK(cudaMemcpyAsync(C.stage.p, host, bytes, cudaMemcpyHostToDevice, C.st));
         src = C.stage.p;
@@ -820,7 +819,7 @@ static void set_spins_range(Ctx &C, System &S, int first, int n, const double *h
 static void get_spins_range(Ctx &C, System &S, int first, int n, double *host) {
     if (n <= 0) return;
     const size_t bytes = (size_t)S.plan.N * 3 * n * sizeof(double);
-    double *dst = bytes < kDirectBytes ? const_cast<double *>(device_view(host)) : nullptr;
+    double *dst = const_cast<double *>(device_view(host));
     const bool direct = dst != nullptr;
     if (!direct) dst = C.stage.p;
     with_args(C, S, [&](auto &a) { launch_gather(a, C.chain_of.p, first, n, dst, C.st); });

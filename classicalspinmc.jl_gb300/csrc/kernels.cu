@@ -516,6 +516,45 @@ __global__ void k_gather(SysArgs<R> a, const int32_t *chain_of, int slot_first, 
     dst[(int64_t)blockIdx.y * 3 * a.n_real + e] = (double)replica(a, r).get1(a.ref2dev[i], (int)(e - 3 * i));
 }
 
+// The same, two consecutive values per thread: 16-byte accesses of the FP64
+// buffer, which cross the host link faster when it is pinned host memory
+// read or written in place.  For blocks of 3 N values that start on 16-byte
+// boundaries (N even, buffer 16-byte aligned).
+template <typename R>
+__global__ void k_scatter2(SysArgs<R> a, const int32_t *chain_of, int slot_first, const double *src) {
+    const int64_t n = 3 * a.n_real, e = 2 * ((int64_t)blockIdx.x * GB + threadIdx.x);
+    if (e >= n) return;
+    const int r = chain_of[slot_first + blockIdx.y] - a.chain_base;
+    const double2 v = *reinterpret_cast<const double2 *>(src + (int64_t)blockIdx.y * n + e);
+    const Spins<R> p = replica(a, r);
+    int64_t i = e / 3;
+    int comp = (int)(e - 3 * i);
+    p.set1(a.ref2dev[i], comp, (R)v.x);
+    if (++comp == 3) {
+        comp = 0;
+        i++;
+    }
+    p.set1(a.ref2dev[i], comp, (R)v.y);
+}
+
+template <typename R>
+__global__ void k_gather2(SysArgs<R> a, const int32_t *chain_of, int slot_first, double *dst) {
+    const int64_t n = 3 * a.n_real, e = 2 * ((int64_t)blockIdx.x * GB + threadIdx.x);
+    if (e >= n) return;
+    const int r = chain_of[slot_first + blockIdx.y] - a.chain_base;
+    const Spins<R> p = replica(a, r);
+    int64_t i = e / 3;
+    int comp = (int)(e - 3 * i);
+    double2 v;
+    v.x = (double)p.get1(a.ref2dev[i], comp);
+    if (++comp == 3) {
+        comp = 0;
+        i++;
+    }
+    v.y = (double)p.get1(a.ref2dev[i], comp);
+    *reinterpret_cast<double2 *>(dst + (int64_t)blockIdx.y * n + e) = v;
+}
+
 // Uniform spins from the INIT stream, counter (reference site, 0, chain, INIT).
 template <typename R>
 __global__ void k_random_spins(SysArgs<R> a, const uint32_t *chain_id, uint32_t k0, uint32_t k1) {
@@ -742,12 +781,18 @@ void launch_exchange(const ChainState &cs, const int2 *lattices, int n_lattices,
 template <typename R>
 void launch_scatter(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, const double *src,
                     cudaStream_t st) {
-    k_scatter<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, src);
+    if (a.n_real % 2 == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+        k_scatter2<R><<<grid_for<R>(3 * a.n_real / 2, n_slots), GB, 0, st>>>(a, chain_of, slot_first, src);
+    else
+        k_scatter<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, src);
 }
 template <typename R>
 void launch_gather(const SysArgs<R> &a, const int32_t *chain_of, int slot_first, int n_slots, double *dst,
                    cudaStream_t st) {
-    k_gather<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, dst);
+    if (a.n_real % 2 == 0 && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0)
+        k_gather2<R><<<grid_for<R>(3 * a.n_real / 2, n_slots), GB, 0, st>>>(a, chain_of, slot_first, dst);
+    else
+        k_gather<R><<<grid_for<R>(3 * a.n_real, n_slots), GB, 0, st>>>(a, chain_of, slot_first, dst);
 }
 template <typename R>
 void launch_random_spins(const SysArgs<R> &a, const uint32_t *chain_id, uint32_t k0, uint32_t k1, cudaStream_t st) {

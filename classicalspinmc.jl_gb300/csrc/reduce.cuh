@@ -23,13 +23,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 __device__ __forceinline__ unsigned warp_sum(unsigned v) { return warp_sum_u(v); }
 
-// The FP64 part of a block sum: v is the sum of the calling thread's warp;
-// the n_warps warps' sums are added by warp 0 (result valid in thread 0).
-// scratch needs n_warps doubles.  Every thread must call it.
-__device__ __forceinline__ double block_sum_warps(double v, double *scratch, int n_warps) {
+// The FP64 part of a block sum: v is the sum of the calling thread's warp
+// (in its own type; lane 0 widens it: FP64 instructions run at a small
+// fraction of the FP32 rate on this device, so no lane does more of them
+// than it must); the n_warps warps' sums are added by warp 0 (result valid in
+// thread 0).  scratch needs n_warps doubles.  Every thread must call it.
+template <typename T> __device__ __forceinline__ double block_sum_warps(T v, double *scratch, int n_warps) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (l == 0) scratch[w] = v;
+    if (l == 0) scratch[w] = (double)v;
     __syncthreads();
     double t = 0.0;
     if (threadIdx.x < 32) {
@@ -46,13 +48,13 @@ __device__ __forceinline__ double block_sum_warps(double v, double *scratch, int
 // is exact), and the warps' sums are added in FP64 -- the FP64 work is per
 // warp, not per thread, since FP64 runs at a small fraction of the FP32 rate.
 template <int NT, typename T> __device__ __forceinline__ double block_sum(T v, double *scratch) {
-    return block_sum_warps((double)warp_sum(v), scratch, NT / 32);
+    return block_sum_warps(warp_sum(v), scratch, NT / 32);
 }
 
 // The same for a block of any multiple of 32 threads (blockDim.x); scratch
 // needs blockDim.x/32 doubles.
 template <typename T> __device__ __forceinline__ double block_sum_any(T v, double *scratch) {
-    return block_sum_warps((double)warp_sum(v), scratch, (int)(blockDim.x >> 5));
+    return block_sum_warps(warp_sum(v), scratch, (int)(blockDim.x >> 5));
 }
 
 // Four sums over a block of any multiple of 32 threads at once (one pass
@@ -61,11 +63,11 @@ template <typename T> __device__ __forceinline__ double block_sum_any(T v, doubl
 template <typename T>
 __device__ __forceinline__ void block_sum4_any(T a, T b, T c, T d, double *scratch, double (&out)[4]) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
-    const double v[4] = {(double)warp_sum(a), (double)warp_sum(b), (double)warp_sum(c), (double)warp_sum(d)};
+    const T v[4] = {warp_sum(a), warp_sum(b), warp_sum(c), warp_sum(d)};
     __syncthreads();
-    if (l == 0)
+    if (l == 0) // widened by lane 0 alone
 #pragma unroll
-        for (int q = 0; q < 4; q++) scratch[q * 32 + w] = v[q];
+        for (int q = 0; q < 4; q++) scratch[q * 32 + w] = (double)v[q];
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 4; q++) {

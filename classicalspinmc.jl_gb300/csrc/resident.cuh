@@ -327,7 +327,7 @@ template <typename R, int CL> struct ResidentCommon {
         }
         double mx, my, mz;
         sy.sum3(ax, ay, az, mx, my, mz);
-        return sqrt(mx * mx + my * my + mz * mz);
+        return threadIdx.x == 0 ? sqrt(mx * mx + my * my + mz * mz) : 0.0;
     }
 
     __device__ void renormalize() const {
@@ -892,8 +892,10 @@ __global__ void __launch_bounds__(NT, 1)
                     if (measure) {
                         double o[4];
                         sync.sum4(meas[0], meas[1], meas[2], meas[3], o);
-                        if (threadIdx.x == 0) E = o[0];
-                        M = sqrt(o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+                        if (threadIdx.x == 0) { // the totals are thread 0's (FP64 in one lane only)
+                            E = o[0];
+                            M = sqrt(o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+                        }
                         have_M = true;
                     } else if (needE) {
                         const double e = k.energy();
