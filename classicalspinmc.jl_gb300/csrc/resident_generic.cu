@@ -3,7 +3,34 @@
 #include "launch.hpp"
 #include "resident.cuh"
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 namespace csmc {
+
+// The host-side attributes a launch needs, looked up once: the dynamic
+// shared memory a kernel is allowed (set per device and kernel, raised when a
+// launch needs more) and the resident capacity of a (kernel, block, shared
+// memory, cluster) shape.  The driver's occupancy queries cost microseconds
+// per call, paid on every run otherwise.
+namespace {
+std::mutex g_attr_mu;
+std::map<std::pair<int, const void *>, size_t> g_smem_allowed;
+std::map<std::tuple<int, const void *, int, size_t, int, int>, int> g_capacity;
+
+cudaError_t allow_smem(const void *fn, size_t smem) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    auto it = g_smem_allowed.find({dev, fn});
+    if (it != g_smem_allowed.end() && it->second >= smem) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) g_smem_allowed[{dev, fn}] = smem;
+    return e;
+}
+} // namespace
 
 template <typename R> static const void *pick(const ResidentSel &sel) {
     if (!sel.fast) return resident_kernel_generic<R>(sel.cub, sel.qua, sel.cl);
@@ -20,7 +47,7 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
     if (block < 32 || block > resident_max_threads(sel.fast, sel.bil, sel.ons) || block % 32 != 0)
         return cudaErrorInvalidValue;
     const void *fn = pick<R>(sel);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_smem(fn, smem);
     if (e != cudaSuccess) return e;
     ChainState csv = cs;
     RunDesc rdv = rd;
@@ -53,9 +80,9 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
 }
 
 // Resident CTAs (cl = 1) or clusters (cl > 1) that fit on the device at once.
-template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms) {
-    const void *fn = pick<R>(sel);
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+template <typename R> static int resident_capacity_query(const void *fn, int block, size_t smem,
+                                                          const ResidentSel &sel, int n_sms) {
+    if (allow_smem(fn, smem) != cudaSuccess) return 0;
     if (sel.cl <= 1) {
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 0;
@@ -74,6 +101,24 @@ template <typename R> int resident_capacity(int block, size_t smem, const Reside
     cfg.numAttrs = 1;
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) return 0;
+    return n;
+}
+
+template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms) {
+    const void *fn = pick<R>(sel);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    const auto key = std::make_tuple(dev, fn, block, smem, sel.cl, n_sms);
+    {
+        std::lock_guard<std::mutex> lock(g_attr_mu);
+        auto it = g_capacity.find(key);
+        if (it != g_capacity.end()) return it->second;
+    }
+    const int n = resident_capacity_query<R>(fn, block, smem, sel, n_sms);
+    if (n > 0) {
+        std::lock_guard<std::mutex> lock(g_attr_mu);
+        g_capacity[key] = n;
+    }
     return n;
 }
 
