@@ -17,7 +17,8 @@
 //    hardware sincos; the sites' positions read from the packed tiles one
 //    chunk ahead) and store their TF32 halves in shared memory in the
 //    no-swizzle K-major core-matrix layout (three phase stages; a quarter-warp
-//    writes one 128-byte core-matrix column, so the stores are conflict-free);
+//    writes one 128-byte core-matrix column, so the stores are conflict-free;
+//    one barrier arrival per warp);
 //  * one issuer warp brings each chunk's spins -- split and laid out the same
 //    way beforehand by k_sf_pack, one layout for every wavevector tile -- by
 //    one bulk copy three chunks ahead (five buffers), and, once the chunk's
@@ -62,7 +63,7 @@ constexpr int SPAD = TC_M + 4;
 constexpr uint32_t STAGE_SMEM = 2 * TC_N * SPAD * 4; // 198 KB
 constexpr uint32_t TC_SMEM = PIPE_SMEM > STAGE_SMEM ? PIPE_SMEM : STAGE_SMEM; // one CTA per SM, which
                                                                              // takes all 512 TMEM columns
-static_assert(TC_SMEM <= 227 * 1024, "shared memory of one CTA");
+static_assert(TC_SMEM + 1024 <= 227 * 1024, "shared memory of one CTA (with its static barriers)");
 // the copy of chunk c + B_AHEAD reuses the buffer of chunk c + B_AHEAD - B_STAGES,
 // whose MMAs the issuer waits for; that chunk must precede c
 static_assert(B_STAGES > B_AHEAD, "a spin buffer is refilled only after the MMAs that read it");
@@ -99,6 +100,12 @@ __device__ __forceinline__ float to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return __uint_as_float(r);
+}
+// The same rounding (to nearest, ties away from zero, on the magnitude) with
+// two integer operations: add half a TF32 unit in the last place to the bits
+// and clear the 13 bits below the TF32 mantissa.  For finite x.
+__device__ __forceinline__ float tf32_hi(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 __device__ __forceinline__ uint64_t gtimer() {
@@ -222,7 +229,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (tid == 0) {
         for (int q = 0; q < B_STAGES; q++) mbar_init_(&bar_b[q], 1);
         for (int q = 0; q < A_STAGES; q++) {
-            mbar_init_(&bar_full[q], TC_PRODUCERS);
+            mbar_init_(&bar_full[q], TC_PRODUCERS / 32); // one arrival per producer warp
             mbar_init_(&bar_mma[q], 1);
         }
         s_fail = 0;
@@ -274,7 +281,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             bool ok = true;
             if (c >= A_STAGES) // the MMAs of chunk c - A_STAGES have read this phase stage
                 ok = mbar_wait(&bar_mma[s], (uint32_t)(((c - A_STAGES) / A_STAGES) & 1));
-            if (!ok || *(volatile int *)&s_fail) {
+            // decided per warp: the warp arrives on the chunk's barrier as one
+            if (!__all_sync(0xffffffffu, ok && !*(volatile int *)&s_fail)) {
                 s_fail = 1;
                 break;
             }
@@ -285,19 +293,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const float t = __fmaf_rn(kz, r.z, __fmaf_rn(ky, r.y, __fmul_rn(kx, r.x)));
                 float sv, cv;
                 sincos_tc(t, &sv, &cv);
-                hc[e] = to_tf32(cv);
-                lc[e] = to_tf32(cv - hc[e]);
-                hs[e] = to_tf32(sv);
-                ls[e] = to_tf32(sv - hs[e]);
+                // hi: the phase rounded to TF32; lo: the exact remainder, of
+                // which the MMA reads the TF32 part (|lo| <= 2^-11 |x|, so the
+                // pair carries x to ~2^-21 of |x|)
+                hc[e] = tf32_hi(cv);
+                lc[e] = __fsub_rn(cv, hc[e]);
+                hs[e] = tf32_hi(sv);
+                ls[e] = __fsub_rn(sv, hs[e]);
             }
             unsigned char *st = a_st + s * A_STAGE;
             *reinterpret_cast<float4 *>(st + 0 * A_BYTES + off) = make_float4(hc[0], hc[1], hc[2], hc[3]);
             *reinterpret_cast<float4 *>(st + 1 * A_BYTES + off) = make_float4(lc[0], lc[1], lc[2], lc[3]);
             *reinterpret_cast<float4 *>(st + 2 * A_BYTES + off) = make_float4(hs[0], hs[1], hs[2], hs[3]);
             *reinterpret_cast<float4 *>(st + 3 * A_BYTES + off) = make_float4(ls[0], ls[1], ls[2], ls[3]);
-            // visible to the tensor cores, then counted
+            // every lane's stores visible to the tensor cores, then the warp counted once
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar_full[s])) : "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar_full[s])) : "memory");
         }
     } else if (lane == 0) { // the issuer
         int copied = -1, landed = -1, issued = 0;
