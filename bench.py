@@ -176,9 +176,9 @@ def bench_ours(args, rank, world, dist):
     elif not args.no_autotune and not args.block:
         # the library's autotuner picks CTAs per replica and threads per CTA on
         # these replicas (state restored exactly afterwards)
-        entries = (L.TuneEntry * 32)()
+        entries = (L.TuneEntry * 64)()
         n = C.c_int32()
-        ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 32, C.byref(n))
+        ctx.call("csmc_autotune", C.byref(run_params(L, 1, 0)), 8, entries, 64, C.byref(n))
         tuned = [{"path": "global" if e.path == L.PATH_GLOBAL else "resident", "cluster": e.cluster,
                   "block": e.block, "persistent": bool(e.persistent),
                   "ms_per_window": round(e.ms_per_window, 5), "chosen": bool(e.chosen)} for e in entries[:n.value]]
@@ -405,9 +405,9 @@ def bench_other(args):
         rp.sweep_start, rp.n_sweeps, rp.t_thermalization = 1, 0, 0
         rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = kw["or_rate"], kw["swap_rate"], kw["probe_rate"]
         rp.kind, rp.path = kind, RUN_PATH
-        entries = (L.TuneEntry * 32)()
+        entries = (L.TuneEntry * 64)()
         n = C.c_int32()
-        ctx.call("csmc_autotune", C.byref(rp), 4, entries, 32, C.byref(n))
+        ctx.call("csmc_autotune", C.byref(rp), 4, entries, 64, C.byref(n))
         tuned = [{"path": "global" if e.path == L.PATH_GLOBAL else "resident", "cluster": e.cluster,
                   "block": e.block, "persistent": bool(e.persistent), "ms_per_window": round(e.ms_per_window, 5),
                   "chosen": bool(e.chosen)} for e in entries[:n.value]]

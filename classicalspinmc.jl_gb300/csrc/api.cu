@@ -977,16 +977,8 @@ static int choose_path(Ctx &C, int requested, int kind) {
 // every thread the same number of sites of the largest colour-class part
 // between two barriers, and the generic kernel its maximum.  The autotuner's
 // block applies to a context of one group.
-static int resident_block(Ctx &C, const Group &G, int hint) {
-    const ResidentSel sel = resident_selection(C, G);
-    int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
-    if (C.size_groups && C.group_block_cap >= 32) mx = std::min(mx, C.group_block_cap);
-    if (hint == 0 && C.block_pref > 0 && !C.size_groups) hint = C.block_pref;
-    if (hint > 0) {
-        require(hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
-        return std::min(hint, mx);
-    }
-    if (!sel.fast) return mx;
+// The most sites of one colour class any CTA of the group holds.
+static int64_t resident_class_sites(const Ctx &C, const Group &G) {
     int64_t n = 32;
     for (int k : G.sys) {
         const System &S = *C.sys[k];
@@ -998,8 +990,27 @@ static int resident_block(Ctx &C, const Group &G, int hint) {
                 n = std::max(n, P.col_count[col]);
         }
     }
-    const int64_t iters = (n + mx - 1) / mx;
+    return n;
+}
+
+// Threads per CTA that cover n sites of a colour class in `extra` more rounds
+// than the fewest the largest block mx needs, as evenly as whole warps allow.
+static int balanced_block(int64_t n, int mx, int extra) {
+    const int64_t iters = (n + mx - 1) / mx + extra;
     return (int)std::min<int64_t>(mx, (n + 32 * iters - 1) / (32 * iters) * 32);
+}
+
+static int resident_block(Ctx &C, const Group &G, int hint) {
+    const ResidentSel sel = resident_selection(C, G);
+    int mx = resident_max_threads(sel.fast, sel.bil, sel.ons);
+    if (C.size_groups && C.group_block_cap >= 32) mx = std::min(mx, C.group_block_cap);
+    if (hint == 0 && C.block_pref > 0 && !C.size_groups) hint = C.block_pref;
+    if (hint > 0) {
+        require(hint % 32 == 0, CSMC_ERR_INVALID, "resident block must be a multiple of 32");
+        return std::min(hint, mx);
+    }
+    if (!sel.fast) return mx;
+    return balanced_block(resident_class_sites(C, G), mx, 0);
 }
 
 // The resident kernel for the lattices of a group: the specialised one when
@@ -2077,10 +2088,20 @@ static void autotune(Ctx &C, const csmc_run_params *p, int n_windows, csmc_tune_
         upload_resident(C);
         C.block_pref = 0;
         const ResidentSel sel = resident_selection(C, *C.groups[0]);
+        // the balanced block (fewest rounds per colour class), the balanced
+        // blocks of one and two rounds more (fewer warps, each with more
+        // registers and less waiting at the class barriers), the largest
         const int balanced = resident_block(C, *C.groups[0], 0),
                   largest = resident_max_threads(sel.fast, sel.bil, sel.ons);
         std::vector<int> blocks{balanced};
-        if (largest != balanced) blocks.push_back(largest);
+        if (sel.fast) {
+            const int64_t n = resident_class_sites(C, *C.groups[0]);
+            for (int extra : {1, 2}) {
+                const int b = balanced_block(n, largest, extra);
+                if (b >= 128 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
+            }
+        }
+        if (std::find(blocks.begin(), blocks.end(), largest) == blocks.end()) blocks.push_back(largest);
         for (int block : blocks) {
             for (bool pers : {true, false}) {
                 if (pers && !(allow_persistent && C.persistent_ok)) continue;

@@ -571,7 +571,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
         return k + (int)blockDim.x < n ? word(st + k + (int)blockDim.x) : make_uint4(0u, 0u, 0u, 0u);
     }
 
-    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], uint4 w) const {
+    __device__ __forceinline__ V3<R> gather(int col, const R (&J)[W], uint4 w, V3<R> init = {R(0), R(0), R(0)}) const {
         const uint32_t v[8] = {w.x & 0xFFFFu, w.x >> 16, w.y & 0xFFFFu, w.y >> 16,
                                w.z & 0xFFFFu, w.z >> 16, w.w & 0xFFFFu, w.w >> 16};
         V3<R> s[W];
@@ -589,28 +589,43 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 else s[t] = sp.get((int)v[t]);
             }
         }
-        V3<R> hb = {R(0), R(0), R(0)};
+        V3<R> hb = init;
 #pragma unroll
         for (int t = 0; t < W; t++) accumulate(hb, col, t, J, s[t]);
         return hb;
     }
 
+    // the onsite part of the local field added to acc: diagonal terms by one
+    // fused multiply-add per component, general matrices by add_matvec
+    __device__ __forceinline__ V3<R> add_onsite(V3<R> acc, const R (&m)[9], V3<R> s) const {
+        using F = Fp<R>;
+        if (ONS == 0) return acc;
+        if (ONS == 1) return {F::fma(m[0], s.x, acc.x), F::fma(m[4], s.y, acc.y), F::fma(m[8], s.z, acc.z)};
+        return add_matvec(acc, m, s);
+    }
+
+    // overrelaxation (monte_carlo.jl:128-137): H = A s + sum_t J_t s_t - h,
+    // accumulated from -h; a site without field (|H|^2 = 0) keeps its spin
     __device__ void or_sweep() const {
+        using F = Fp<R>;
         for (int col = 0; col < S.n_colours; col++) {
             R J[W], a[9];
             V3<R> h;
             load_coef(col, OFF_A, J, a, h);
+            const V3<R> nh = {-h.x, -h.y, -h.z};
             const int st = this->col_begin(col), n = this->col_size(col);
             uint4 wn = first_word(st, n);
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
                 const int d = st + k;
                 const uint4 w = wn;
                 wn = next_word(st, n, k);
-                const V3<R> hb = gather(col, J, w);
+                const V3<R> hb = gather(col, J, w, nh);
                 const V3<R> s = sp.get(d);
-                const V3<R> H = vsub(vadd(onsite(a, s), hb), h);
-                if (H.x == R(0) && H.y == R(0) && H.z == R(0)) continue;
-                sp.set(d, reflect(s, H, true));
+                const V3<R> H = add_onsite(hb, a, s);
+                const R den = dot(H, H);
+                if (den == R(0)) continue;
+                const R proj = Math<R>::div_(F::mul(R(2), dot(s, H)), den);
+                sp.set(d, {F::fma(proj, H.x, -s.x), F::fma(proj, H.y, -s.y), F::fma(proj, H.z, -s.z)});
             }
             this->sy.bar();
         }

@@ -253,7 +253,7 @@ function c_persistent(ctx)
     check(ccall((:csmc_persistent, libcsmc), Cint, (Ptr{Cvoid}, Ref{Int32}), ctx, r))
     r[] != 0
 end
-function c_autotune(ctx, p::CsmcRunParams, n_windows::Integer; capacity::Integer=32)
+function c_autotune(ctx, p::CsmcRunParams, n_windows::Integer; capacity::Integer=64)
     entries = Vector{CsmcTuneEntry}(undef, capacity)
     n = Ref{Int32}(0)
     check(ccall((:csmc_autotune, libcsmc), Cint,

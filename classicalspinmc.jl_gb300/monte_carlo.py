@@ -603,13 +603,14 @@ def autotune(mc: MonteCarlo, n_windows: int = 4, alg: _Alg | None = None) -> lis
     rp.probe_rate = p.probe_rate
     rp.kind = alg.kind
     rp.path = _PATHS[mc.path]
-    entries = (_lib.TuneEntry * 16)()
+    cap = 64  # more than the candidates the library tries
+    entries = (_lib.TuneEntry * cap)()
     n = C.c_int32()
-    mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, 16, C.byref(n))
+    mc.ctx.call("csmc_autotune", C.byref(rp), int(n_windows), entries, cap, C.byref(n))
     paths = {_lib.PATH_RESIDENT: "resident", _lib.PATH_GLOBAL: "global"}
     return [{"path": paths.get(e.path, "resident"), "cluster": e.cluster, "block": e.block,
              "persistent": bool(e.persistent),
-             "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)} for e in entries[:n.value]]
+             "ms_per_window": e.ms_per_window, "chosen": bool(e.chosen)} for e in entries[:min(n.value, cap)]]
 
 
 def _print_runtime_statistics(mc, t, acc, exc, n):
