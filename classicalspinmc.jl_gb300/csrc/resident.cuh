@@ -1026,6 +1026,20 @@ template <typename R, int W, int BIL, int ONS> const void *resident_fast_for(int
     if (cl == 2) return resident_fast_kernel<R, W, BIL, ONS, 2>();
     return resident_fast_kernel<R, W, BIL, ONS, 1>();
 }
+// The same scalar-coupling kernels (whose full build is bound to 896 threads
+// and so to 72 registers a thread) bound to at most kNarrowThreads threads
+// per CTA: up to 85 registers a thread, for launches of that many threads or
+// fewer.  Defined for the widths a resident_fast_<precision>_w<W>_narrow.cu
+// instantiates; elsewhere (and for other coupling classes) nullptr.
+constexpr int kNarrowThreads = 768;
+template <typename R, int W> const void *resident_kernel_fast_narrow(int bil, int ons, int cl);
+template <typename R, int W, int ONS> const void *resident_fast_narrow_for(int cl) {
+    static_assert(resident_max_threads(true, 0, ONS) > kNarrowThreads, "a narrower bound than the full build");
+    if (cl == 4) return (const void *)k_resident<ResidentFast<R, 0, ONS, W, 4>, R, kNarrowThreads, 4>;
+    if (cl == 2) return (const void *)k_resident<ResidentFast<R, 0, ONS, W, 2>, R, kNarrowThreads, 2>;
+    return (const void *)k_resident<ResidentFast<R, 0, ONS, W, 1>, R, kNarrowThreads, 1>;
+}
+
 template <typename R, int W> const void *resident_fast_table(int bil, int ons, int cl) {
     if (bil == 0)
         return ons == 0 ? resident_fast_for<R, W, 0, 0>(cl)

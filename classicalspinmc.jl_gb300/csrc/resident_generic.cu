@@ -32,8 +32,14 @@ cudaError_t allow_smem(const void *fn, size_t smem) {
 }
 } // namespace
 
-template <typename R> static const void *pick(const ResidentSel &sel) {
+// The kernel of a selection; `block` > 0: the threads per CTA of the launch,
+// which may take a build bound to fewer threads (more registers per thread).
+template <typename R> static const void *pick(const ResidentSel &sel, int block = 0) {
     if (!sel.fast) return resident_kernel_generic<R>(sel.cub, sel.qua, sel.cl);
+    if constexpr (sizeof(R) == 4) {
+        if (block > 0 && block <= kNarrowThreads && sel.width > 4 && sel.width <= 6)
+            if (const void *fn = resident_kernel_fast_narrow<float, 6>(sel.bil, sel.ons, sel.cl)) return fn;
+    }
     if (sel.width <= 4) return resident_kernel_fast<R, 4>(sel.bil, sel.ons, sel.cl);
     if (sel.width <= 6) return resident_kernel_fast<R, 6>(sel.bil, sel.ons, sel.cl);
     return resident_kernel_fast<R, 8>(sel.bil, sel.ons, sel.cl);
@@ -46,7 +52,7 @@ cudaError_t launch_resident(const ResSys<R> *d_sys, const int2 *items, int n_ite
     // work_ctr must be zero when the kernel starts (the caller resets it on `st`)
     if (block < 32 || block > resident_max_threads(sel.fast, sel.bil, sel.ons) || block % 32 != 0)
         return cudaErrorInvalidValue;
-    const void *fn = pick<R>(sel);
+    const void *fn = pick<R>(sel, block);
     cudaError_t e = allow_smem(fn, smem);
     if (e != cudaSuccess) return e;
     ChainState csv = cs;
@@ -105,7 +111,7 @@ template <typename R> static int resident_capacity_query(const void *fn, int blo
 }
 
 template <typename R> int resident_capacity(int block, size_t smem, const ResidentSel &sel, int n_sms) {
-    const void *fn = pick<R>(sel);
+    const void *fn = pick<R>(sel, block);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     const auto key = std::make_tuple(dev, fn, block, smem, sel.cl, n_sms);
