@@ -379,6 +379,7 @@ static void upload_system(Ctx &C, System &S) {
         S.fa.cf.Q = S.fQ.p;
         S.fa.cf.E2 = S.fE2.p;
         S.fa.cf.Js = S.fJs.p;
+        S.fa.cf.iso2 = S.bil_class == 0 ? 1 : 0;
         S.fa.S = (float)P.desc.S;
     } else {
         const size_t nsp = (size_t)S.R * 3 * Np; // x | y | z blocks
@@ -405,6 +406,7 @@ static void upload_system(Ctx &C, System &S) {
         S.da.cf.Q = S.dQ.p;
         S.da.cf.E2 = S.dE2.p;
         S.da.cf.Js = S.dJs.p;
+        S.da.cf.iso2 = S.bil_class == 0 ? 1 : 0;
         S.da.S = P.desc.S;
     }
 }

@@ -30,14 +30,10 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, u
                                                      uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-#ifdef __CUDA_ARCH__
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-#else
-        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
-        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-#endif
+        // each 32 x 32 -> 64-bit product as one wide multiply (both halves)
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
         uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
         c0 = n0;
         c1 = lo1;
@@ -74,6 +70,10 @@ template <typename R> struct Coef {
     // O+P (dE), O+P/2 (energy share), and the scalar of each bilinear slot
     // when every coupling is a multiple of the identity
     const R *A, *Q, *E2, *Js;
+    // 1: every bilinear coupling of the lattice is c I, and Js[b * W2 + t]
+    // holds its c (the same value as miso's) -- one table read per partner
+    // instead of the coupling id and its isotropy record
+    int32_t iso2;
     // per tensor id: isotropic bilinear {flag, J}, cubic {flag, kappa},
     // quartic {flag, q1, q2, q3}
     const R *miso, *ciso, *qiso;
@@ -176,6 +176,10 @@ __device__ __forceinline__ void partner_fields(const Tab<Idx> &tb, const Coef<R>
     const int Np = (int)tb.Np, di = (int)d;
     // one term of each kind, its partner spins given
     auto bil = [&](int t, V3<R> sj) {
+        if (cf.iso2) { // block-uniform
+            hb = add_scaled(hb, cf.Js[b * tb.W2 + t], sj);
+            return;
+        }
         const int id = cf.c2[b * tb.W2 + t];
         if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sj); // J I
         else hb = add_matvec(hb, cf.mats + 9 * id, sj);
@@ -292,6 +296,10 @@ __device__ __forceinline__ void bilinear_fields2(const Tab<uint32_t> &tb, const 
     hb1 = {R(0), R(0), R(0)};
     const int Np = (int)tb.Np;
     auto bil = [&](int b, int t, V3<R> sj, V3<R> &hb) {
+        if (cf.iso2) { // block-uniform
+            hb = add_scaled(hb, cf.Js[b * tb.W2 + t], sj);
+            return;
+        }
         const int id = cf.c2[b * tb.W2 + t];
         if (cf.miso[2 * id] != R(0)) hb = add_scaled(hb, cf.miso[2 * id + 1], sj); // J I
         else hb = add_matvec(hb, cf.mats + 9 * id, sj);
