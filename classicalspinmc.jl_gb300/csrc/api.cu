@@ -281,6 +281,10 @@ static void upload_system(Ctx &C, System &S) {
     }
     S.cub = P.W3 > 0;
     S.qua = P.W4 > 0;
+    int ons_diag = 1;
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 9; k++)
+            if (k % 4 != 0 && (O[b * 9 + k] != 0.0 || Pm[b * 9 + k] != 0.0)) ons_diag = 0;
     // per pattern: 2O+P (local field), O+P (dE), O+P/2 (energy share)
     std::vector<double> A((nb + 1) * 9, 0.0), Qm((nb + 1) * 9, 0.0), E2((nb + 1) * 9, 0.0);
     for (int k = 0; k < (nb + 1) * 9; k++) {
@@ -380,6 +384,7 @@ static void upload_system(Ctx &C, System &S) {
         S.fa.cf.E2 = S.fE2.p;
         S.fa.cf.Js = S.fJs.p;
         S.fa.cf.iso2 = S.bil_class == 0 ? 1 : 0;
+        S.fa.cf.ons_diag = ons_diag;
         S.fa.S = (float)P.desc.S;
     } else {
         const size_t nsp = (size_t)S.R * 3 * Np; // x | y | z blocks
@@ -407,6 +412,7 @@ static void upload_system(Ctx &C, System &S) {
         S.da.cf.E2 = S.dE2.p;
         S.da.cf.Js = S.dJs.p;
         S.da.cf.iso2 = S.bil_class == 0 ? 1 : 0;
+        S.da.cf.ons_diag = ons_diag;
         S.da.S = P.desc.S;
     }
 }

@@ -74,6 +74,10 @@ template <typename R> struct Coef {
     // holds its c (the same value as miso's) -- one table read per partner
     // instead of the coupling id and its isotropy record
     int32_t iso2;
+    // 1: every pattern's onsite matrix O and self-loop matrix P is diagonal;
+    // the onsite products then read and multiply the diagonals alone (the
+    // zero off-diagonal terms of the full products add nothing)
+    int32_t ons_diag;
     // per tensor id: isotropic bilinear {flag, J}, cubic {flag, kappa},
     // quartic {flag, q1, q2, q3}
     const R *miso, *ciso, *qiso;
@@ -337,6 +341,12 @@ template <typename R> __device__ __forceinline__ V3<R> matvec(const R *M, V3<R> 
             F::fma(M[5], s.z, F::fma(M[4], s.y, F::mul(M[3], s.x))),
             F::fma(M[8], s.z, F::fma(M[7], s.y, F::mul(M[6], s.x)))};
 }
+// matvec of a diagonal matrix: M[0] s.x, M[4] s.y, M[8] s.z -- the values
+// matvec gives when the off-diagonal entries are zero
+template <typename R> __device__ __forceinline__ V3<R> diagvec(const R *M, V3<R> s) {
+    using F = Fp<R>;
+    return {F::mul(M[0], s.x), F::mul(M[4], s.y), F::mul(M[8], s.z)};
+}
 template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) {
     using F = Fp<R>;
     return F::fma(a.z, b.z, F::fma(a.y, b.y, F::mul(a.x, b.x)));
@@ -346,7 +356,8 @@ template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) {
 // partners' fields: 2 O s + (self loops) + hb + hc + hq - h.
 template <typename R>
 __device__ __forceinline__ V3<R> field_of(const Coef<R> &cf, int b, V3<R> s, V3<R> hb, V3<R> hc, V3<R> hq) {
-    const V3<R> os = matvec(cf.O + 9 * b, s), ps = matvec(cf.P + 9 * b, s);
+    const V3<R> os = cf.ons_diag ? diagvec(cf.O + 9 * b, s) : matvec(cf.O + 9 * b, s),
+                ps = cf.ons_diag ? diagvec(cf.P + 9 * b, s) : matvec(cf.P + 9 * b, s);
     const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
     const V3<R> two_os = {Fp<R>::mul(R(2), os.x), Fp<R>::mul(R(2), os.y), Fp<R>::mul(R(2), os.z)};
     return vsub(vadd(vadd(vadd(vadd(two_os, ps), hb), hc), hq), h);
@@ -368,6 +379,12 @@ __device__ __forceinline__ R delta_e(const Coef<R> &cf, int b, V3<R> s, V3<R> sn
     using F = Fp<R>;
     const R *O = cf.O + 9 * b, *P = cf.P + 9 * b;
     R q[9];
+    if (cf.ons_diag) { // block-uniform
+#pragma unroll
+        for (int k = 0; k < 9; k += 4) q[k] = F::add(O[k], P[k]);
+        const R en = dot(sn, diagvec(q, sn)), eo = dot(s, diagvec(q, s));
+        return F::add(F::sub(en, eo), dot(vsub(sn, s), hext));
+    }
 #pragma unroll
     for (int k = 0; k < 9; k++) q[k] = F::add(O[k], P[k]);
     const R en = dot(sn, matvec(q, sn)), eo = dot(s, matvec(q, s));
