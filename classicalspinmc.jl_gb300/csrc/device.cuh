@@ -354,13 +354,17 @@ template <typename R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) {
 
 // get_local_field (hamiltonian.jl:3-67) of site spin s of pattern b from its
 // partners' fields: 2 O s + (self loops) + hb + hc + hq - h.
-template <typename R>
+// CUB / QUA false: hc / hq are zero and not added (x + 0 is x).
+template <typename R, bool CUB = true, bool QUA = true>
 __device__ __forceinline__ V3<R> field_of(const Coef<R> &cf, int b, V3<R> s, V3<R> hb, V3<R> hc, V3<R> hq) {
     const V3<R> os = cf.ons_diag ? diagvec(cf.O + 9 * b, s) : matvec(cf.O + 9 * b, s),
                 ps = cf.ons_diag ? diagvec(cf.P + 9 * b, s) : matvec(cf.P + 9 * b, s);
     const V3<R> h = {cf.h[3 * b], cf.h[3 * b + 1], cf.h[3 * b + 2]};
     const V3<R> two_os = {Fp<R>::mul(R(2), os.x), Fp<R>::mul(R(2), os.y), Fp<R>::mul(R(2), os.z)};
-    return vsub(vadd(vadd(vadd(vadd(two_os, ps), hb), hc), hq), h);
+    V3<R> f = vadd(vadd(two_os, ps), hb);
+    if (CUB) f = vadd(f, hc);
+    if (QUA) f = vadd(f, hq);
+    return vsub(f, h);
 }
 
 // get_local_field (hamiltonian.jl:3-67) at device site d.
@@ -368,7 +372,7 @@ template <typename R, typename Idx, bool CUB, bool QUA, class SV>
 __device__ __forceinline__ V3<R> local_field(const Tab<Idx> &tb, const Coef<R> &cf, const SV &sv, int64_t d, int b) {
     V3<R> hb, hc, hq;
     partner_fields<R, Idx, CUB, QUA>(tb, cf, sv, d, b, hb, hc, hq);
-    return field_of(cf, b, sv.get(d), hb, hc, hq);
+    return field_of<R, CUB, QUA>(cf, b, sv.get(d), hb, hc, hq);
 }
 
 // Energy of moving site d from s to sn with all other spins fixed:

@@ -71,12 +71,12 @@ __global__ void __launch_bounds__(GB) k_metro_colour(SysArgs<R> a, ChainState cs
             const int bb[2] = {a.tb.pat[dd[0]], a.tb.pat[dd[1]]};
             V3<R> hb[2];
             bilinear_fields2(a.tb, a.cf, p, dd[0], dd[1], bb[0], bb[1], hb[0], hb[1]);
-            const V3<R> z = {R(0), R(0), R(0)};
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 if (q == 1 && !two) break;
                 const int d = dd[q], b = bb[q];
-                const V3<R> hext = vsub(vadd(vadd(hb[q], z), z), V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
+                // no cubic or quartic fields to add (hb + 0 + 0 is hb)
+                const V3<R> hext = vsub(hb[q], V3<R>{a.cf.h[3 * b], a.cf.h[3 * b + 1], a.cf.h[3 * b + 2]});
                 const V3<R> s = p.get(d);
                 const Draw<R> dr((uint32_t)d, msweep, key, a.k0, a.k1);
                 const V3<R> sn = propose<R>(kind, a.S, sigma, s, dr.uphi, dr.uz);
