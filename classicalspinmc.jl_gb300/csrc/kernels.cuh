@@ -112,9 +112,9 @@ struct ResidentSel {
     int cl; // CTAs per replica (thread-block cluster size; 1 = no cluster)
 };
 constexpr int RESIDENT_WMAX = 8; // bilinear slots per site of the specialised kernel
-// Threads per CTA at most of a resident kernel (its launch bound): 1024 for
+// Threads per CTA at most of a resident kernel (its launch bound): 896 for
 // the specialised kernel with scalar couplings and at most diagonal onsite
-// terms (64 registers per thread suffice), else 512.
+// terms (72 registers per thread), else 512.
 __host__ __device__ constexpr int resident_max_threads(bool fast, int bil, int ons) {
     return fast && bil == 0 && ons < 2 ? 896 : 512;
 }
