@@ -187,7 +187,11 @@ int csmc_lattice_info_of(void *ctx, int32_t lattice, csmc_lattice_info *info);
 /* lattice.spins of one slot, reference layout (lattice.jl:293-301). */
 int csmc_set_spins(void *ctx, int32_t slot, const double *spins);
 int csmc_get_spins(void *ctx, int32_t slot, double *spins);
-/* All slots, concatenated in slot order. */
+/* All slots, concatenated in slot order.  Pinned (page-locked or registered)
+ * host buffers are read or written in place by the layout-conversion kernel
+ * across the host link; pageable ones go through one bulk copy to a device
+ * staging buffer.  Both return after the host buffer has been read (set) or
+ * written (get). */
 int csmc_set_spins_all(void *ctx, const double *spins);
 int csmc_get_spins_all(void *ctx, double *spins);
 /* Uniform random spins of length S from the Philox INIT stream
