@@ -647,6 +647,7 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
             V3<R> h;
             load_coef(col, OFF_Q, J, q, h);
             if (MEASURE) load_coef(col, OFF_E2, J, e2, h);
+            const V3<R> nh = {-h.x, -h.y, -h.z};
             const bool bonds = MEASURE && col == 1;
             const int st = this->col_begin(col), n = this->col_size(col);
             uint4 wn = first_word(st, n);
@@ -655,9 +656,8 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                 const uint4 w = wn;
                 wn = next_word(st, n, k);
                 const uint32_t dg = (uint32_t)this->device_index(col, d);
-                const V3<R> hb = gather(col, J, w);
+                const V3<R> hext = gather(col, J, w, nh); // hb - h, accumulated from -h
                 const V3<R> s = sp.get(d);
-                const V3<R> hext = vsub(hb, h);
                 const Draw<R> dr(dg, msweep, this->key, S.k0, S.k1);
                 const V3<R> sn = propose<R>(kind, S.S, sigma, s, dr.uphi, dr.uz);
                 using F = Fp<R>;
@@ -668,10 +668,10 @@ template <typename R, int BIL, int ONS, int W, int CL> struct ResidentFast : Res
                     sp.set(d, sn);
                     acc++;
                 }
-                if (MEASURE) {
+                if (MEASURE) { // class 1: s.E2.s + s.(hb - h); class 0: s.E2.s - s.h
                     const V3<R> f = accept ? sn : s;
-                    R part = F::sub(dot(f, onsite(e2, f)), dot(f, h));
-                    if (bonds) part = F::add(part, dot(f, hb));
+                    const R part = bonds ? F::add(dot(f, onsite(e2, f)), dot(f, hext))
+                                         : F::sub(dot(f, onsite(e2, f)), dot(f, h));
                     pe = F::add(pe, part);
                     pmx = F::add(pmx, f.x);
                     pmy = F::add(pmy, f.y);
