@@ -144,6 +144,7 @@ struct Ctx {
     cudaStream_t st = nullptr;
     DevBuf<int32_t> slot_of, chain_of;
     DevBuf<double> T_slot, sigma_slot, acc_slot, exch_slot, E_chain, M_chain, last_acc;
+    DevBuf<double> E_win; // persistent windows: energies by slot, two alternating buffers
     DevBuf<double> T_stash; // mc.T of every slot during a csmc_metropolis_sweep_at call
     DevBuf<float> invT_slot, invT_stash; // (float)(1 / T) per slot (single-precision sweeps)
     DevBuf<uint32_t> chain_id;           // per chain: the key of its Philox streams
@@ -702,6 +703,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     C->exch_slot.upload(zeros);
     C->E_chain.upload(zeros);
     C->M_chain.upload(zeros);
+    C->E_win.alloc(2 * (size_t)nc);
     C->last_acc.upload(zeros);
     C->lambda_slot.upload(zeros);
     for (auto &S : C->sys) S->cons.lambda_slot = C->lambda_slot.p;
@@ -730,6 +732,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.exch_slot = C->exch_slot.p;
     cs.E_chain = C->E_chain.p;
     cs.M_chain = C->M_chain.p;
+    cs.E_win = C->E_win.p;
     cs.sweep_acc = C->sweep_acc.p;
     cs.drift_bits = C->drift_bits.p;
     cs.error_flag = C->error_flag.p;

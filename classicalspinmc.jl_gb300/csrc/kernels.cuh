@@ -22,6 +22,7 @@ struct ChainState {
     unsigned int *drift_bits;      // max relative |S| error, float bits
     int *error_flag;               // nonzero: a bounded wait gave up
     const uint32_t *chain_id;      // per chain: the key of its Philox streams (default: the chain index)
+    double *E_win; // persistent windows: each window's last energy by slot, two buffers alternating
 };
 
 // One lattice for the global-memory kernels.
@@ -179,6 +180,34 @@ __device__ __forceinline__ void exchange_slots(const ChainState &cs, int sys, in
             cs.exch_slot[sb] = __ldcg(cs.exch_slot + sb) + 1;
         }
     }
+}
+
+// The same exchange seen from one replica, in slot `slot` of a lattice of
+// slots [slot_base, slot_base + n_rep): the pair of this iteration that holds
+// the slot (pairs start at relative slot `phase`), the decision of
+// exchange_slots for it -- the same formula, draw and operands, with the
+// energies of the pair's slots taken from E_slot (the energy of the chain in
+// each slot) -- and the slot the replica holds afterwards.  Both replicas of
+// a pair reach the same decision, each on its own.  *swapped: the pair was
+// exchanged.
+__device__ __forceinline__ int exchange_partner(const ChainState &cs, const double *E_slot, int sys, int slot_base,
+                                                int n_rep, int slot, int64_t it, int swap_rate, uint32_t k0,
+                                                uint32_t k1, bool *swapped) {
+    *swapped = false;
+    const int rel = slot - slot_base;
+    const int phase = (int)((it / swap_rate) % 2);
+    if (rel < phase) return slot;
+    const int a = phase + 2 * ((rel - phase) / 2), b = a + 1;
+    if (b >= n_rep) return slot;
+    const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
+    const int se = slot_base + ev, so = slot_base + od;
+    const double Te = __ldcg(cs.T_slot + se), To = __ldcg(cs.T_slot + so);
+    const double Ee = __ldcg(E_slot + se), Eo = __ldcg(E_slot + so);
+    const double x = exp((1 / To - 1 / Te) * (Eo - Ee));
+    const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, (uint32_t)sys ^ (uint32_t)(it >> 32), PURPOSE_SWAP, k0, k1);
+    if (!(u53(w.x, w.y) < (x < 1.0 ? x : 1.0))) return slot;
+    *swapped = true;
+    return slot_base + (rel == a ? b : a);
 }
 
 // Probe record kq of one lattice's slots (monte_carlo.jl:368-370): the energy

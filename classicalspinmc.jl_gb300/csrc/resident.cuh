@@ -735,6 +735,7 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ uint32_t s_vote;
     __shared__ double s_sigma, s_T;
     __shared__ R s_invT;
+    __shared__ int s_slot;
     __shared__ ResSys<R> s_sys;
     __shared__ R s_coef[K::kCoefSmem];
     uint32_t parity = 0;
@@ -839,6 +840,7 @@ __global__ void __launch_bounds__(NT, 1)
         const uint64_t every = rd.renorm_every > 0 ? (uint64_t)rd.renorm_every : 0;
         uint64_t next_renorm = every ? (sweeps / every + 1) * every : 0;
         unsigned int epoch = 0;
+        int cur_slot = -1; // persistent windows: the slot after the last exchange (-1: read it)
 
         for (int64_t w0 = rd.it0; w0 < rd.it1;) {
             // the window [w0, w1): the whole launch, or (persistent) up to the
@@ -851,7 +853,7 @@ __global__ void __launch_bounds__(NT, 1)
                 const int64_t q = (w0 + rd.swap_period - 1) / rd.swap_period * rd.swap_period;
                 if (q + 1 < w1) w1 = q + 1;
             }
-            const int slot = __ldcg(cs.slot_of + c);
+            const int slot = cur_slot >= 0 ? cur_slot : __ldcg(cs.slot_of + c);
             // T and 1/T by thread 0 (FP64 division runs at a small fraction of
             // the FP32 rate on this device)
             if (threadIdx.x == 0) {
@@ -941,31 +943,50 @@ __global__ void __launch_bounds__(NT, 1)
                 const double at = sync.sum(acc_thread);
                 if (threadIdx.x == 0) acc_total = at;
             }
+            const int64_t last = w1 - 1;
+            const bool exchange = rd.persistent && rd.swap_enabled && last % rd.swap_period == 0;
+            // the window's energy by slot, for the exchange (buffers alternate
+            // by window: a buffer is rewritten only two windows later, after a
+            // grid barrier that every reader of it has passed)
+            double *const E_slot = cs.E_win + (int64_t)((last / (rd.swap_period > 0 ? rd.swap_period : 1)) & 1) * rd.n_slots;
             if (writer) {
                 cs.E_chain[c] = E;
                 cs.acc_slot[slot] = __ldcg(cs.acc_slot + slot) + acc_total;
                 cs.sigma_slot[slot] = s_sigma;
+                if (exchange) E_slot[slot] = E;
             }
-            const int64_t last = w1 - 1;
             w0 = w1;
-            if (!rd.persistent || !rd.swap_enabled || last % rd.swap_period != 0) break;
-            // exchange of every lattice by block 0 between two grid barriers,
-            // then the probe record of the exchange iteration
-            // a barrier that gave up (timeout, or another CTA's error) ends the
-            // launch; the ranks of a cluster decide together
+            if (!exchange) break;
+            // every window's energies written, then each replica takes the
+            // exchange of its own pair (the same decision as its partner's)
+            // and moves to its new slot: one grid barrier per window, no CTA
+            // reads a value another writes before the next barrier.  A barrier
+            // that gave up (timeout, or another CTA's error) ends the launch;
+            // the ranks of a cluster decide together.
             if (!cluster_all<CL>(grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok), &s_vote)) break;
-            if (blockIdx.x == 0) {
-                for (int L = 0; L < rd.n_lattices; L++)
-                    exchange_slots(cs, L, rd.lattices[L].x, rd.lattices[L].y, last, rd.swap_rate, rd.k0, rd.k1);
-                if (is_probe(rd, last)) {
-                    const int64_t kq = (last - rd.probe_first) / rd.probe_rate;
-                    __syncthreads();
-                    if (kq >= 0 && kq < rd.probe_cap)
-                        for (int L = 0; L < rd.n_lattices; L++)
-                            record_slots(cs, rd.lattices[L].x, rd.lattices[L].y, rd.rec_E, rd.rec_M, kq, rd.n_slots);
+            if (threadIdx.x == 0) {
+                const int2 lat = rd.lattices[w.x];
+                bool swapped = false;
+                const int ns = exchange_partner(cs, E_slot, w.x, lat.x, lat.y, slot, last, rd.swap_rate, rd.k0, rd.k1,
+                                                &swapped);
+                if (rank == 0) { // the chain's records (each slot has one writer)
+                    if (swapped) {
+                        cs.exch_slot[slot] = __ldcg(cs.exch_slot + slot) + 1;
+                        cs.slot_of[c] = ns;
+                        cs.chain_of[ns] = c;
+                    }
+                    if (is_probe(rd, last)) { // the probe record of the exchange iteration, by the new slot
+                        const int64_t kq = (last - rd.probe_first) / rd.probe_rate;
+                        if (kq >= 0 && kq < rd.probe_cap) {
+                            if (rd.rec_E) rd.rec_E[kq * rd.n_slots + ns] = E;
+                            if (rd.rec_M) rd.rec_M[kq * rd.n_slots + ns] = cs.M_chain[c];
+                        }
+                    }
                 }
+                s_slot = ns;
             }
-            if (!cluster_all<CL>(grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok), &s_vote)) break;
+            __syncthreads();
+            cur_slot = s_slot;
         }
         // every thread's shared-memory accesses are ordered before the bulk
         // copies that follow (the stores below, the next item's staging)
