@@ -57,20 +57,22 @@ template <typename T> __device__ __forceinline__ double block_sum_any(T v, doubl
     return block_sum_warps(warp_sum(v), scratch, (int)(blockDim.x >> 5));
 }
 
-// Four sums over a block of any multiple of 32 threads at once (one pass
-// through shared memory); results valid in thread 0.  scratch needs 4 x 32
+// N sums over a block of any multiple of 32 threads at once (one pass
+// through shared memory); results valid in thread 0.  scratch needs N x 32
 // doubles.  Same order per value as block_sum_any.
-template <typename T>
-__device__ __forceinline__ void block_sum4_any(T a, T b, T c, T d, double *scratch, double (&out)[4]) {
+template <int N, typename T>
+__device__ __forceinline__ void block_sumn_any(const T (&x)[N], double *scratch, double (&out)[N]) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
-    const T v[4] = {warp_sum(a), warp_sum(b), warp_sum(c), warp_sum(d)};
+    T v[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) v[q] = warp_sum(x[q]);
     __syncthreads();
     if (l == 0) // widened by lane 0 alone
 #pragma unroll
-        for (int q = 0; q < 4; q++) scratch[q * 32 + w] = (double)v[q];
+        for (int q = 0; q < N; q++) scratch[q * 32 + w] = (double)v[q];
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < N; q++) {
         double t = 0.0;
         if (threadIdx.x < 32) {
             t = l < nw ? scratch[q * 32 + l] : 0.0;

@@ -228,7 +228,8 @@ template <typename R> __host__ __device__ constexpr int64_t spin_smem_bytes(int6
 // Block (CL = 1) or cluster barrier and sums; totals valid in thread 0 of
 // every CTA, identical on all ranks (same summation order).
 template <int CL> struct Sync {
-    double *scratch, *red; // scratch: 4 x 32 doubles; red: 4 doubles (cluster exchange)
+    double *scratch, *red; // scratch: kSums x 32 doubles; red: kSums doubles (cluster exchange)
+    static constexpr int kSums = 5; // the most values summed at once
     int *error_flag;
     // Barrier between colour classes: the block, or every thread of the
     // cluster (hardware cluster barrier, release/acquire at cluster scope, so
@@ -249,21 +250,23 @@ template <int CL> struct Sync {
         cluster_sync_all();
         return tot;
     }
-    // four totals at once (the energy and the magnetisation of a measuring sweep)
-    template <typename T> __device__ void sum4(T x0, T x1, T x2, T x3, double (&o)[4]) const {
-        block_sum4_any(x0, x1, x2, x3, scratch, o);
+    // N totals at once (the energy, the magnetisation and the accepted
+    // proposals of a measuring sweep)
+    template <int N, typename T> __device__ void sumn(const T (&x)[N], double (&o)[N]) const {
+        static_assert(N <= kSums, "scratch holds kSums values");
+        block_sumn_any<N>(x, scratch, o);
         if (CL == 1) return;
         if (threadIdx.x == 0)
 #pragma unroll
-            for (int q = 0; q < 4; q++) red[q] = o[q];
+            for (int q = 0; q < N; q++) red[q] = o[q];
         cluster_sync_all();
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int q = 0; q < 4; q++) o[q] = 0.0;
+            for (int q = 0; q < N; q++) o[q] = 0.0;
             for (int r = 0; r < CL; r++) {
                 const uint32_t base = map_rank(smem_u32(red), r);
 #pragma unroll
-                for (int q = 0; q < 4; q++) o[q] += ld_cluster(base + 8 * q, 0.0);
+                for (int q = 0; q < N; q++) o[q] += ld_cluster(base + 8 * q, 0.0);
             }
         }
         cluster_sync_all();
@@ -728,8 +731,8 @@ __global__ void __launch_bounds__(NT, 1)
                ChainState cs, RunDesc rd) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t bar;
-    __shared__ double scratch[4 * 32];
-    __shared__ double red[4];
+    __shared__ double scratch[Sync<CL>::kSums * 32];
+    __shared__ double red[Sync<CL>::kSums];
     __shared__ int s_item;
     __shared__ int s_ok;
     __shared__ uint32_t s_vote;
@@ -854,12 +857,14 @@ __global__ void __launch_bounds__(NT, 1)
                 if (q + 1 < w1) w1 = q + 1;
             }
             const int slot = cur_slot >= 0 ? cur_slot : __ldcg(cs.slot_of + c);
-            // T and 1/T by thread 0 (FP64 division runs at a small fraction of
-            // the FP32 rate on this device)
-            if (threadIdx.x == 0) {
+            // T, 1/T and sigma of the slot by thread 0, unless the exchange
+            // that ended the previous window took them already.  Single
+            // precision reads 1/T formed on the host (the same value: FP64
+            // division runs at a small fraction of the FP32 rate here).
+            if (threadIdx.x == 0 && cur_slot < 0) {
                 s_sigma = (rd.reset_sigma && w0 == rd.it0) ? rd.sigma0 : __ldcg(cs.sigma_slot + slot);
                 s_T = rd.T_override > 0 ? rd.T_override : __ldcg(cs.T_slot + slot);
-                s_invT = (R)(1.0 / s_T);
+                s_invT = (sizeof(R) == 4 && rd.T_override <= 0) ? (R)__ldcg(cs.invT_slot + slot) : (R)(1.0 / s_T);
             }
             __syncthreads();
             const double T = s_T;
@@ -870,6 +875,7 @@ __global__ void __launch_bounds__(NT, 1)
             // kind needs the rate, else once at the end of the window
             const bool adaptive = rd.kind == CSMC_METROPOLIS_ADAPTIVE;
             unsigned acc_thread = 0;
+            bool acc_summed = false; // the window's accepted proposals already summed (measuring sweep)
 
             for (int64_t it = w0; it < w1; it++) {
                 if (rd.or_rate != 0) {
@@ -907,8 +913,22 @@ __global__ void __launch_bounds__(NT, 1)
                         acc_thread += a;
                     }
                     if (measure) {
-                        double o[4];
-                        sync.sum4(meas[0], meas[1], meas[2], meas[3], o);
+                        // the window's last Metropolis sweep also sums the
+                        // window's accepted proposals (small integers: exact
+                        // in the value type and in FP64)
+                        const bool with_acc = !adaptive && it + dosweep >= w1;
+                        double o[5];
+                        if (with_acc) {
+                            const R x[5] = {meas[0], meas[1], meas[2], meas[3], (R)acc_thread};
+                            sync.sumn<5>(x, o);
+                            acc_summed = true;
+                            if (threadIdx.x == 0) acc_total = o[4];
+                        } else {
+                            const R x[4] = {meas[0], meas[1], meas[2], meas[3]};
+                            double o4[4];
+                            sync.sumn<4>(x, o4);
+                            for (int q = 0; q < 4; q++) o[q] = o4[q];
+                        }
                         if (threadIdx.x == 0) { // the totals are thread 0's (FP64 in one lane only)
                             E = o[0];
                             M = sqrt(o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
@@ -939,7 +959,7 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
 
-            if (!adaptive) {
+            if (!adaptive && !acc_summed) {
                 const double at = sync.sum(acc_thread);
                 if (threadIdx.x == 0) acc_total = at;
             }
@@ -951,7 +971,9 @@ __global__ void __launch_bounds__(NT, 1)
             double *const E_slot = cs.E_win + (int64_t)((last / (rd.swap_period > 0 ? rd.swap_period : 1)) & 1) * rd.n_slots;
             if (writer) {
                 cs.E_chain[c] = E;
-                cs.acc_slot[slot] = __ldcg(cs.acc_slot + slot) + acc_total;
+                // one owner adds to a slot's counters per window, windows in
+                // order: the additions need no read here (and keep their order)
+                atomicAdd(cs.acc_slot + slot, acc_total);
                 cs.sigma_slot[slot] = s_sigma;
                 if (exchange) E_slot[slot] = E;
             }
@@ -971,7 +993,7 @@ __global__ void __launch_bounds__(NT, 1)
                                                 &swapped);
                 if (rank == 0) { // the chain's records (each slot has one writer)
                     if (swapped) {
-                        cs.exch_slot[slot] = __ldcg(cs.exch_slot + slot) + 1;
+                        atomicAdd(cs.exch_slot + slot, 1.0);
                         cs.slot_of[c] = ns;
                         cs.chain_of[ns] = c;
                     }
@@ -984,6 +1006,11 @@ __global__ void __launch_bounds__(NT, 1)
                     }
                 }
                 s_slot = ns;
+                if (swapped) { // the new slot's T, 1/T and sigma for the next window
+                    s_sigma = __ldcg(cs.sigma_slot + ns);
+                    s_T = __ldcg(cs.T_slot + ns);
+                    s_invT = sizeof(R) == 4 ? (R)__ldcg(cs.invT_slot + ns) : (R)(1.0 / s_T);
+                }
             }
             __syncthreads();
             cur_slot = s_slot;
