@@ -147,6 +147,7 @@ struct Ctx {
     DevBuf<double> E_win; // persistent windows: energies by slot, two alternating buffers
     DevBuf<double> T_stash; // mc.T of every slot during a csmc_metropolis_sweep_at call
     DevBuf<float> invT_slot, invT_stash; // (float)(1 / T) per slot (single-precision sweeps)
+    DevBuf<double> invT64_slot;          // 1 / T per slot (the persistent exchange's exponent)
     DevBuf<uint32_t> chain_id;           // per chain: the key of its Philox streams
     DevBuf<unsigned long long> sweep_acc;
     DevBuf<unsigned int> drift_bits;
@@ -698,6 +699,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     std::vector<float> fones(nc, 1.0f);
     C->invT_slot.upload(fones);
     C->invT_stash.upload(fones);
+    C->invT64_slot.upload(ones);
     C->sigma_slot.upload(sig);
     C->acc_slot.upload(zeros);
     C->exch_slot.upload(zeros);
@@ -727,6 +729,7 @@ static Ctx *create(const csmc_lattice_desc *descs, int n, const int32_t *reps, i
     cs.chain_of = C->chain_of.p;
     cs.T_slot = C->T_slot.p;
     cs.invT_slot = C->invT_slot.p;
+    cs.invT64_slot = C->invT64_slot.p;
     cs.sigma_slot = C->sigma_slot.p;
     cs.acc_slot = C->acc_slot.p;
     cs.exch_slot = C->exch_slot.p;
@@ -1633,6 +1636,9 @@ int csmc_set_temperatures(void *c, const double *T) {
     CK(cudaMemcpy(C.T_slot.p, T, C.n_chains * sizeof(double), cudaMemcpyHostToDevice));
     const std::vector<float> inv = reciprocals(T, C.n_chains);
     CK(cudaMemcpy(C.invT_slot.p, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice));
+    std::vector<double> inv64((size_t)C.n_chains);
+    for (int k = 0; k < C.n_chains; k++) inv64[k] = 1.0 / T[k];
+    CK(cudaMemcpy(C.invT64_slot.p, inv64.data(), inv64.size() * sizeof(double), cudaMemcpyHostToDevice));
     std::vector<int32_t> ident(C.n_chains);
     std::iota(ident.begin(), ident.end(), 0);
     CK(cudaMemcpy(C.slot_of.p, ident.data(), ident.size() * sizeof(int32_t), cudaMemcpyHostToDevice));

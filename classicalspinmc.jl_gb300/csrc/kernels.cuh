@@ -16,6 +16,7 @@ struct ChainState {
     int32_t *chain_of; // slot -> chain
     double *T_slot, *sigma_slot;
     float *invT_slot;  // (float)(1 / T) per slot, formed on the host
+    const double *invT64_slot; // 1 / T per slot in FP64, formed on the host (the same bits as a division here)
     double *acc_slot, *exch_slot;
     double *E_chain, *M_chain;
     unsigned long long *sweep_acc; // accepted proposals of the current sweep, per chain
@@ -190,24 +191,33 @@ __device__ __forceinline__ void exchange_slots(const ChainState &cs, int sys, in
 // each slot) -- and the slot the replica holds afterwards.  Both replicas of
 // a pair reach the same decision, each on its own.  *swapped: the pair was
 // exchanged.
+// The slot paired with `slot` at exchange iteration `it` (pairs of relative
+// slots (phase + 2m, phase + 2m + 1)), or -1.
+__device__ __forceinline__ int exchange_pair_slot(int slot_base, int n_rep, int slot, int64_t it, int swap_rate) {
+    const int rel = slot - slot_base;
+    const int phase = (int)((it / swap_rate) % 2);
+    if (rel < phase) return -1;
+    const int a = phase + 2 * ((rel - phase) / 2), b = a + 1;
+    if (b >= n_rep) return -1;
+    return slot_base + (rel == a ? b : a);
+}
 __device__ __forceinline__ int exchange_partner(const ChainState &cs, const double *E_slot, int sys, int slot_base,
                                                 int n_rep, int slot, int64_t it, int swap_rate, uint32_t k0,
                                                 uint32_t k1, bool *swapped) {
     *swapped = false;
-    const int rel = slot - slot_base;
-    const int phase = (int)((it / swap_rate) % 2);
-    if (rel < phase) return slot;
-    const int a = phase + 2 * ((rel - phase) / 2), b = a + 1;
-    if (b >= n_rep) return slot;
+    const int ps = exchange_pair_slot(slot_base, n_rep, slot, it, swap_rate);
+    if (ps < 0) return slot;
+    const int a = (slot < ps ? slot : ps) - slot_base, b = a + 1;
     const int ev = (a % 2 == 0) ? a : b, od = (ev == a) ? b : a;
     const int se = slot_base + ev, so = slot_base + od;
-    const double Te = __ldcg(cs.T_slot + se), To = __ldcg(cs.T_slot + so);
+    // 1/To - 1/Te from reciprocals formed on the host: the bits of the divisions
+    const double iTe = __ldcg(cs.invT64_slot + se), iTo = __ldcg(cs.invT64_slot + so);
     const double Ee = __ldcg(E_slot + se), Eo = __ldcg(E_slot + so);
-    const double x = exp((1 / To - 1 / Te) * (Eo - Ee));
+    const double x = exp((iTo - iTe) * (Eo - Ee));
     const U4 w = philox4x32_10((uint32_t)a, (uint32_t)it, (uint32_t)sys ^ (uint32_t)(it >> 32), PURPOSE_SWAP, k0, k1);
     if (!(u53(w.x, w.y) < (x < 1.0 ? x : 1.0))) return slot;
     *swapped = true;
-    return slot_base + (rel == a ? b : a);
+    return ps;
 }
 
 // Probe record kq of one lattice's slots (monte_carlo.jl:368-370): the energy

@@ -988,6 +988,15 @@ __global__ void __launch_bounds__(NT, 1)
             if (!cluster_all<CL>(grid_barrier(rd.grid_bar, rd.n_blocks, epoch, cs.error_flag, &s_ok), &s_vote)) break;
             if (threadIdx.x == 0) {
                 const int2 lat = rd.lattices[w.x];
+                // the partner slot's T, 1/T and sigma, loaded beside the decision's operands
+                const int ps = exchange_pair_slot(lat.x, lat.y, slot, last, rd.swap_rate);
+                double p_sigma = 0.0, p_T = 1.0;
+                R p_invT = R(1);
+                if (ps >= 0) {
+                    p_sigma = __ldcg(cs.sigma_slot + ps);
+                    p_T = __ldcg(cs.T_slot + ps);
+                    p_invT = sizeof(R) == 4 ? (R)__ldcg(cs.invT_slot + ps) : (R)__ldcg(cs.invT64_slot + ps);
+                }
                 bool swapped = false;
                 const int ns = exchange_partner(cs, E_slot, w.x, lat.x, lat.y, slot, last, rd.swap_rate, rd.k0, rd.k1,
                                                 &swapped);
@@ -1007,9 +1016,9 @@ __global__ void __launch_bounds__(NT, 1)
                 }
                 s_slot = ns;
                 if (swapped) { // the new slot's T, 1/T and sigma for the next window
-                    s_sigma = __ldcg(cs.sigma_slot + ns);
-                    s_T = __ldcg(cs.T_slot + ns);
-                    s_invT = sizeof(R) == 4 ? (R)__ldcg(cs.invT_slot + ns) : (R)(1.0 / s_T);
+                    s_sigma = p_sigma;
+                    s_T = p_T;
+                    s_invT = p_invT;
                 }
             }
             __syncthreads();
