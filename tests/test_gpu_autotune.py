@@ -65,9 +65,10 @@ def _set_persistent(mc, on):
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("name", ["sc", "honeycomb", "triangular_open", "pyrochlore"])
 def test_persistent_windows_equal_one_launch_per_window(m, orc, name, precision):
-    """Exchange windows in one cooperative launch (grid barriers, exchange by
-    block 0) give the same chain, records and counters as one launch per
-    window with a separate exchange launch."""
+    """Exchange windows in one cooperative launch (one grid barrier per
+    window, each replica deciding its own pair's exchange) give the same
+    chain, records and counters as one launch per window with a separate
+    exchange launch."""
     res = []
     for on in (False, True):
         lat, _, mc = setup(m, orc, name, precision, R=4, seed=9)
@@ -98,3 +99,49 @@ def test_autotune_automatic_path_also_times_the_global_sweeps(m, orc):
     for r in range(2):
         s = mc.spins(r)
         assert abs(m.total_energy(mc, r) - ol.total_energy(np.asfortranarray(s))) <= 1e-4 * lat.size
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_persistent_exchange_of_several_lattices(m, precision):
+    """Two lattices of different sizes with three replicas each in one
+    context, parallel tempering in one cooperative launch: each replica takes
+    its own pair's exchange within its lattice's slots (monte_carlo.jl:308-349),
+    and the chains, probe records and accepted and exchange counters equal
+    those of one launch per window with the stand-alone exchange kernel; both
+    lattices exchange."""
+    import ctypes as C
+    from importlib import import_module
+    L = import_module(m.__name__ + "._lib")
+    E = m.examples
+    lats = [m.Lattice((6, 6), E.triangular_afm(h=0.2), 1.0, rng=np.random.default_rng(6)),
+            m.Lattice((8, 8), E.triangular_afm(h=0.5), 1.0, rng=np.random.default_rng(8))]
+    T = np.array([0.50, 0.52, 0.54, 0.60, 0.62, 0.64])  # close rungs: exchanges are frequent
+    n_slots, cap = 6, 16
+    res = []
+    for on in (0, 1):
+        ctx = m.monte_carlo.Context(lats, [3, 3], precision=precision, seed=5)
+        ctx.set_temperatures(T)
+        for k in range(n_slots):
+            ctx.set_spins(k, lats[k // 3].spins)
+        ctx.call("csmc_set_persistent", on)
+        rec_E, rec_M = np.zeros((cap, n_slots)), np.zeros((cap, n_slots))
+        acc, exch = np.zeros(n_slots), np.zeros(n_slots)
+        rp = L.RunParams()
+        rp.sweep_start, rp.n_sweeps, rp.t_thermalization = 1, 60, 0
+        rp.overrelaxation_rate, rp.swap_rate, rp.probe_rate = 2, 4, 4
+        rp.kind, rp.path = L.METROPOLIS, L.PATH_RESIDENT
+        rp.probe_energy = rec_E.ctypes.data_as(C.POINTER(C.c_double))
+        rp.probe_magnetization = rec_M.ctypes.data_as(C.POINTER(C.c_double))
+        rp.probe_capacity = cap
+        rp.accepted = acc.ctypes.data_as(C.POINTER(C.c_double))
+        rp.exchanged = exch.ctypes.data_as(C.POINTER(C.c_double))
+        ctx.call("csmc_run", C.byref(rp))
+        res.append(([ctx.get_spins(k) for k in range(n_slots)], rec_E, rec_M, acc, exch, rp.n_probes_out))
+    ref, got = res
+    for k in range(n_slots):
+        assert np.abs(ref[0][k] - got[0][k]).max() <= 1e-12 * (1 if precision == "fp64" else 1e6), k
+    assert ref[5] == got[5] == 15  # probes at iterations 4, 8, ..., 60
+    assert np.abs(ref[1] - got[1]).max() <= obs_tol(precision) * 64
+    assert np.abs(ref[2] - got[2]).max() <= obs_tol(precision) * 64
+    assert np.array_equal(ref[3], got[3]) and np.array_equal(ref[4], got[4])
+    assert got[4][:3].sum() > 0 and got[4][3:].sum() > 0  # both lattices exchanged
