@@ -64,6 +64,7 @@ constexpr uint32_t STAGE_SMEM = 2 * TC_N * SPAD * 4; // 198 KB
 constexpr uint32_t TC_SMEM = PIPE_SMEM > STAGE_SMEM ? PIPE_SMEM : STAGE_SMEM; // one CTA per SM, which
                                                                              // takes all 512 TMEM columns
 static_assert(TC_SMEM + 1024 <= 227 * 1024, "shared memory of one CTA (with its static barriers)");
+static_assert(TC_SMEM + 1024 < (1u << 18), "descriptor address fields (address / 16, 14 bits) do not carry");
 // the copy of chunk c + B_AHEAD reuses the buffer of chunk c + B_AHEAD - B_STAGES,
 // whose MMAs the issuer waits for; that chunk must precede c
 static_assert(B_STAGES > B_AHEAD, "a spin buffer is refilled only after the MMAs that read it");
@@ -314,6 +315,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else if (lane == 0) { // the issuer
         int copied = -1, landed = -1, issued = 0;
+        const uint64_t desc_a0 = smem_desc(smem_addr(a_st)), desc_b0 = smem_desc(smem_addr(b_st));
         auto copy_chunk = [&](int cc) {
             const int q = cc % B_STAGES;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b[q])),
@@ -343,15 +345,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             landed = c;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t abase = smem_addr(a_st + s * A_STAGE), bbase = smem_addr(b_st + q * B_STAGE);
+            // the operands' descriptors: the stage's base descriptor plus the
+            // byte offset / 16 (shared addresses stay below 256 KB, so the
+            // 14-bit address field never carries)
+            const uint64_t da = desc_a0 + (uint64_t)((s * A_STAGE) >> 4), db = desc_b0 + (uint64_t)((q * B_STAGE) >> 4);
 #pragma unroll
             for (int j = 0; j < TC_K / 8; j++) { // K-steps of 8 sites: two core-matrix columns
-                const uint32_t kofs = j * 2 * LBO;
-                const uint64_t bh = smem_desc(bbase + kofs), bl = smem_desc(bbase + B_BYTES + kofs);
+                const uint64_t kd = (uint64_t)((j * 2 * LBO) >> 4);
+                const uint64_t bh = db + kd, bl = db + (B_BYTES >> 4) + kd;
 #pragma unroll
                 for (int ph = 0; ph < 2; ph++) { // cos, sin
-                    const uint64_t ah = smem_desc(abase + (2 * ph) * A_BYTES + kofs);
-                    const uint64_t al = smem_desc(abase + (2 * ph + 1) * A_BYTES + kofs);
+                    const uint64_t ah = da + (uint64_t)(((2 * ph) * A_BYTES) >> 4) + kd;
+                    const uint64_t al = da + (uint64_t)(((2 * ph + 1) * A_BYTES) >> 4) + kd;
                     const uint32_t d = tmem + (ph ? SIN_COL : 0u);
                     const uint32_t first = (c == 0 && j == 0) ? 0u : 1u; // accumulate after the first
                     const uint64_t aa[3] = {ah, ah, al}, bb[3] = {bh, bl, bh};
