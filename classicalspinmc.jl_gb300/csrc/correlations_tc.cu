@@ -147,6 +147,20 @@ __device__ __forceinline__ void sincos_tc(float t, float *s, float *c) {
     __sincosf(r, s, c);
 }
 
+// Buffer index and barrier phase of consecutive chunks in a ring of N
+// buffers: chunk c has idx = c % N and phase = (c / N) & 1; next() steps to
+// c + 1 (no division on the loops' paths).
+template <int N> struct Ring {
+    int idx = 0;
+    uint32_t phase = 0;
+    __device__ __forceinline__ void next() {
+        if (++idx == N) {
+            idx = 0;
+            phase ^= 1u;
+        }
+    }
+};
+
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[24], int at) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(v[at]), "=r"(v[at + 1]), "=r"(v[at + 2]), "=r"(v[at + 3]), "=r"(v[at + 4]), "=r"(v[at + 5]),
@@ -273,15 +287,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         };
         float4 pn[4];
         if (n_my > 0) positions(0, pn);
-        for (int c = 0; c < n_my; c++) {
-            const int s = c % A_STAGES;
+        Ring<A_STAGES> ra; // chunk c's phase stage
+        for (int c = 0; c < n_my; c++, ra.next()) {
+            const int s = ra.idx;
             float4 pc[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) pc[e] = pn[e];
             if (c + 1 < n_my) positions(c + 1, pn);
             bool ok = true;
-            if (c >= A_STAGES) // the MMAs of chunk c - A_STAGES have read this phase stage
-                ok = mbar_wait(&bar_mma[s], (uint32_t)(((c - A_STAGES) / A_STAGES) & 1));
+            if (c >= A_STAGES) // the MMAs of chunk c - A_STAGES (same stage, previous phase) have read it
+                ok = mbar_wait(&bar_mma[s], ra.phase ^ 1u);
             // decided per warp: the warp arrives on the chunk's barrier as one
             if (!__all_sync(0xffffffffu, ok && !*(volatile int *)&s_fail)) {
                 s_fail = 1;
@@ -316,8 +331,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (lane == 0) { // the issuer
         int copied = -1, landed = -1, issued = 0;
         const uint64_t desc_a0 = smem_desc(smem_addr(a_st)), desc_b0 = smem_desc(smem_addr(b_st));
+        Ring<B_STAGES> rcopy; // the spin buffer of the next chunk to copy
         auto copy_chunk = [&](int cc) {
-            const int q = cc % B_STAGES;
+            const int q = rcopy.idx;
+            rcopy.next();
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b[q])),
                          "r"(B_STAGE)
                          : "memory");
@@ -329,16 +346,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             copied = cc;
         };
         for (int cc = 0; cc < B_AHEAD && cc < n_my; cc++) copy_chunk(cc);
-        for (int c = 0; c < n_my; c++) {
-            const int s = c % A_STAGES, q = c % B_STAGES;
+        Ring<A_STAGES> ra, rj; // chunk c's phase stage; that of chunk j = c + B_AHEAD - B_STAGES
+        Ring<B_STAGES> rb;     // chunk c's spin buffer
+        for (int c = 0; c < n_my; c++, ra.next(), rb.next()) {
+            const int s = ra.idx, q = rb.idx;
             bool ok = true;
             if (c + B_AHEAD < n_my) {
                 const int j = c + B_AHEAD - B_STAGES; // the chunk whose buffer the copy reuses
-                if (j >= 0) ok = mbar_wait(&bar_mma[j % A_STAGES], (uint32_t)((j / A_STAGES) & 1));
+                if (j >= 0) {
+                    ok = mbar_wait(&bar_mma[rj.idx], rj.phase);
+                    rj.next();
+                }
                 if (ok) copy_chunk(c + B_AHEAD);
             }
-            ok = ok && mbar_wait(&bar_full[s], (uint32_t)((c / A_STAGES) & 1));
-            ok = ok && mbar_wait(&bar_b[q], (uint32_t)((c / B_STAGES) & 1));
+            ok = ok && mbar_wait(&bar_full[s], ra.phase);
+            ok = ok && mbar_wait(&bar_b[q], rb.phase);
             if (!ok || *(volatile int *)&s_fail) {
                 s_fail = 1;
                 break;
