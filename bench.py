@@ -257,15 +257,18 @@ def bench_ours(args, rank, world, dist):
     rec_E = np.zeros((cap, R_REPL))
     rec_M = np.zeros((cap, R_REPL))
     e2e_steps = max(3, min(args.steps, args.e2e_steps))
+    rp = run_params(L, it, ITER_PER_STEP, rec_E, rec_M, cap)  # one parameter block, advanced per step
+    p_in, p_out = h_in.ctypes.data_as(C.POINTER(C.c_double)), h_out.ctypes.data_as(C.POINTER(C.c_double))
     for k in range(e2e_steps + 2):
         if k == 2:
             barrier()
             t0 = time.perf_counter()
-        ctx.call("csmc_set_spins_all", h_in.ctypes.data_as(C.POINTER(C.c_double)))
-        ctx.call("csmc_run", C.byref(run_params(L, it, ITER_PER_STEP, rec_E, rec_M, cap)))
+        ctx.call("csmc_set_spins_all", p_in)
+        rp.sweep_start = it
+        ctx.call("csmc_run", C.byref(rp))
         it += ITER_PER_STEP
-        ctx.call("csmc_get_spins_all", h_out.ctypes.data_as(C.POINTER(C.c_double)))
-        h_in, h_out = h_out, h_in
+        ctx.call("csmc_get_spins_all", p_out)
+        p_in, p_out = p_out, p_in
     barrier()
     t_e2e = time.perf_counter() - t0
     out["e2e"] = {"value": world * upd * e2e_steps / t_e2e, "unit": "site updates/s",
