@@ -139,8 +139,8 @@ struct RunDesc {
     int32_t swap_enabled;
     // persistent mode: the launch covers every window of [it0, it1) (a window
     // ends at an exchange iteration, a multiple of swap_period); between
-    // windows all CTAs meet at a grid barrier, block 0 runs the exchange of
-    // every lattice and the probe record, and all CTAs meet again
+    // windows all CTAs meet at one grid barrier, then each replica takes the
+    // exchange of its own pair (exchange_partner) and writes its own records
     int32_t persistent;
     int32_t n_lattices;
     int64_t swap_period;      // lcm(swap_rate, max(or_rate, 1)): iterations that exchange

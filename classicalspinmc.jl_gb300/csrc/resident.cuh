@@ -8,8 +8,9 @@
 // barrier between classes, and written back once (single precision: bulk
 // TMA stores).  A persistent launch (cooperative, every replica resident)
 // runs many exchange windows: the replicas stay in shared memory, and between
-// windows all CTAs meet at a bounded grid barrier while block 0 performs the
-// replica exchange (monte_carlo.jl:308-349) and the probe record.
+// windows all CTAs meet at one bounded grid barrier, after which each replica
+// takes the exchange of its own pair (monte_carlo.jl:308-349; both replicas of
+// a pair reach the same decision) and writes its own probe record.
 //
 // Shared-memory layout: the replica's spins in the device layout (single
 // precision: one float4 per site; double: x | y | z blocks), then, for the

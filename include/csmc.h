@@ -379,10 +379,11 @@ int csmc_selftest_timeout(void *ctx, int32_t which);
  * in the reference).  On (the default): when every replica of the context is
  * resident on the device at once, csmc_run runs up to 128 exchange windows in
  * one cooperative launch of the resident kernel, whose blocks meet at a
- * bounded grid barrier after each window while block 0 performs the replica
- * exchange and the probe record; the replicas stay in shared memory across
- * windows.  Off, or if the device refuses the cooperative launch: one launch
- * per window and a separate exchange launch.  Both give the same chain.
+ * bounded grid barrier after each window, after which each replica takes the
+ * exchange of its own pair (the same decision as its partner's) and writes
+ * its own probe record; the replicas stay in shared memory across windows.
+ * Off, or if the device refuses the cooperative launch: one launch per window
+ * and a separate exchange launch.  Both give the same chain.
  * csmc_persistent reports whether persistent launches are in use. */
 int csmc_set_persistent(void *ctx, int32_t on);
 int csmc_persistent(void *ctx, int32_t *on);
